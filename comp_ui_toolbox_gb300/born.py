@@ -1,0 +1,368 @@
+"""Python host mirror of the reference's Born-operator interface.
+
+Mirrors the calls a user of ``scattering.operator_born`` makes
+(``+scattering/operator_born.m``, ``+scattering/operator.m``):
+
+* ``OperatorBorn.forward(gamma)``   -> ``forward_scalar`` / ``op * gamma``   (``operator_born.m:37-44``, ``:174-238``)
+* ``OperatorBorn.adjoint(u)``       -> ``adjoint_scalar``                    (``operator_born.m:243-320``)
+* ``OperatorBorn.combined_scalar(mode, x)`` -> ``operator.combined_scalar``  (``operator.m:1019-1072``; mode 0 size,
+  1 forward, 2 adjoint)
+* ``OperatorBorn.vjp(gamma, u)``    -> gradient of ``0.5*||Phi gamma - u||^2`` used by the solvers
+  (``operator.m:717``)
+
+All arithmetic runs in ``libcui_born.so`` through its C-ABI (``include/cui_born.h``).
+NumPy inputs take the FP64 host path (``cui_born_combined_host``, the MEX
+semantics); CUDA ``torch`` tensors take the FP32 device path.  There is no CPU
+fallback: without the compiled library every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+__all__ = ["OperatorBorn", "CuiError", "load_library", "BornForward", "born_forward", "launch_count"]
+
+_LIB_PATH = Path(__file__).resolve().parent / "libcui_born.so"
+
+STATUS = {0: "CUI_OK", 1: "CUI_ERR_INVALID_ARG", 2: "CUI_ERR_UNSUPPORTED_SETUP", 3: "CUI_ERR_OOM",
+          4: "CUI_ERR_CUDA", 5: "CUI_ERR_TIMEOUT", 6: "CUI_ERR_NUMERIC", 7: "CUI_ERR_NO_DEVICE"}
+
+# reference MEX error identifiers for each status (+scattering/combined_quick_gpu.cu:201-428, .h:43)
+MEX_ID = {1: "combined_quick_gpu:NoValidDoubleMatrix", 2: "combined_quick_gpu:NoSymmetricGridsSetup",
+          3: "adjoint_quick_gpu:ErrorCUDA", 4: "adjoint_quick_gpu:ErrorCUDA", 5: "adjoint_quick_gpu:ErrorCUDA",
+          6: "combined_quick_gpu:NoComplexDoubles", 7: "combined_quick_gpu:NoCUDADevices"}
+
+
+class CuiError(RuntimeError):
+    """A libcui_born call failed; ``status`` is the cui_status code."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.identifier = MEX_ID.get(status, "combined_quick_gpu:Error")
+        super().__init__(f"{STATUS.get(status, status)}: {message} [{self.identifier}]")
+
+
+class c64(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class MixDesc(C.Structure):
+    _fields_ = [("n_f", C.c_int32), ("indices_f_to_unique", C.POINTER(C.c_int32)),
+                ("n_active", C.c_int32), ("indices_active", C.POINTER(C.c_int32)),
+                ("prefactors", C.c_void_p)]
+
+
+class MeasurementDesc(C.Structure):
+    _fields_ = [("n_f", C.c_int32), ("indices_f_to_unique", C.POINTER(C.c_int32)),
+                ("p_incident", C.c_void_p), ("n_mixes", C.c_int32), ("mixes", C.POINTER(MixDesc))]
+
+
+class BornDesc(C.Structure):
+    _fields_ = [("n_dims", C.c_int32), ("n_points_axis", C.c_int32 * 3), ("n_elements_axis", C.c_int32 * 2),
+                ("n_points_per_pitch", C.c_int32 * 2), ("n_f_unique", C.c_int32), ("table_form", C.c_int32),
+                ("h_ref", C.c_void_p), ("indices_grid_FOV_shift", C.POINTER(C.c_int32)),
+                ("h_lateral", C.c_void_p), ("n_measurements", C.c_int32),
+                ("measurements", C.POINTER(MeasurementDesc)), ("device", C.c_int32)]
+
+
+class BornInfo(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("n_points", "n_observations", "n_elements", "n_slots", "n_f_unique",
+                                         "table_bytes", "incident_bytes", "workspace_bytes", "contraction_macs")]
+
+
+_lib = None
+
+# every symbol include/cui_born.h declares, with its ctypes signature
+_SIGNATURES = {
+    "cui_born_plan_create": (C.c_int, [C.POINTER(BornDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    "cui_born_plan_destroy": (C.c_int, [C.c_void_p]),
+    "cui_born_plan_info": (C.c_int, [C.c_void_p, C.POINTER(BornInfo)]),
+    "cui_born_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cui_born_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
+    "cui_born_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
+    "cui_born_vjp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
+                               C.c_int64, C.c_void_p, C.c_void_p]),
+    "cui_born_combined_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
+                                         C.c_int64]),
+    "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
+                                    C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
+    "cui_status_string": (C.c_char_p, [C.c_int]),
+    "cui_last_error": (C.c_char_p, []),
+    "cui_launch_count": (C.c_int64, []),
+}
+
+
+def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
+    """Load libcui_born.so (built in-tree by ``comp_ui_toolbox_gb300/build.py``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else _LIB_PATH
+    if not p.exists():
+        raise CuiError(4, f"{p} is missing: build it with `python -m comp_ui_toolbox_gb300.build` "
+                          "(the operator has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def launch_count() -> int:
+    """Kernel launches issued by the library in this process."""
+    return int(load_library().cui_launch_count())
+
+
+def _check(status: int):
+    if status != 0:
+        msg = load_library().cui_last_error().decode(errors="replace")
+        raise CuiError(status, msg)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def _c128_f(a) -> np.ndarray:
+    """Complex FP64 array in column-major (MATLAB) order."""
+    return np.asfortranarray(np.asarray(a, dtype=np.complex128))
+
+
+class OperatorBorn:
+    """Persistent GB300 Born operator built from the reference operator's tables.
+
+    Parameters mirror what ``combined_quick_gpu`` reads from
+    ``operator_born`` (``combined_quick_gpu.cu:203-393``):
+
+    * ``n_points_axis``: FOV grid points, lateral axes then axial;
+    * ``n_elements_axis`` / ``n_points_per_pitch``: array elements and grid
+      points per pitch along each lateral axis;
+    * ``h_lateral``: lateral-offset table ``(F, Nz, [No_y,] No_x)``, or
+      ``h_ref`` ``(F, P)`` with ``indices_grid_FOV_shift`` ``(P, E)``
+      (1-based) -- the reference's own symmetric-grid representation;
+    * ``measurements``: sequence of objects or dicts with ``f_idx`` (0-based
+      global frequency indices), ``p_incident`` ``(F_w, P)`` and ``mixes``,
+      each with ``f_idx`` (0-based into the measurement's frequencies),
+      ``active`` (0-based element indices) and ``pref`` ``(F_mix, n_active)``.
+    """
+
+    def __init__(self, *, n_points_axis: Sequence[int], n_elements_axis: Sequence[int],
+                 n_points_per_pitch: Sequence[int], n_f_unique: int, measurements,
+                 h_lateral: Optional[np.ndarray] = None, h_ref: Optional[np.ndarray] = None,
+                 indices_grid_FOV_shift: Optional[np.ndarray] = None, device: int = 0, max_objects: int = 1):
+        lib = load_library()
+        self._lib = lib
+        self._plan = C.c_void_p()
+        keep = []  # host arrays must outlive plan creation only
+        n_dims = len(n_points_axis)
+        d = BornDesc()
+        d.n_dims = n_dims
+        for k, v in enumerate(n_points_axis):
+            d.n_points_axis[k] = int(v)
+        for k, v in enumerate(n_elements_axis):
+            d.n_elements_axis[k] = int(v)
+        for k, v in enumerate(n_points_per_pitch):
+            d.n_points_per_pitch[k] = int(v)
+        d.n_f_unique = int(n_f_unique)
+        if h_lateral is not None:
+            t = np.ascontiguousarray(np.asarray(h_lateral, dtype=np.complex128))
+            keep.append(t)
+            d.table_form = 1
+            d.h_lateral = t.ctypes.data
+        else:
+            if h_ref is None or indices_grid_FOV_shift is None:
+                raise ValueError("give h_lateral, or h_ref together with indices_grid_FOV_shift")
+            h = _c128_f(h_ref)
+            m = np.asfortranarray(np.asarray(indices_grid_FOV_shift, dtype=np.int32))
+            keep += [h, m]
+            d.table_form = 0
+            d.h_ref = h.ctypes.data
+            d.indices_grid_FOV_shift = m.ctypes.data_as(C.POINTER(C.c_int32))
+        meas = (MeasurementDesc * len(measurements))()
+        for w, ms in enumerate(measurements):
+            get = (lambda o, k: o[k]) if isinstance(ms, dict) else getattr
+            f_idx = _i32(np.asarray(get(ms, "f_idx")) + 1)
+            p_in = _c128_f(get(ms, "p_incident"))
+            mixes_in = list(get(ms, "mixes"))
+            mixes = (MixDesc * max(1, len(mixes_in)))()
+            keep += [f_idx, p_in, mixes]
+            for k, mx in enumerate(mixes_in):
+                gm = (lambda o, key: o[key]) if isinstance(mx, dict) else getattr
+                mf = _i32(np.asarray(gm(mx, "f_idx")) + 1)
+                act = _i32(np.asarray(gm(mx, "active")) + 1)
+                pref = _c128_f(gm(mx, "pref"))
+                keep += [mf, act, pref]
+                mixes[k].n_f = len(mf)
+                mixes[k].indices_f_to_unique = mf.ctypes.data_as(C.POINTER(C.c_int32))
+                mixes[k].n_active = len(act)
+                mixes[k].indices_active = act.ctypes.data_as(C.POINTER(C.c_int32))
+                mixes[k].prefactors = pref.ctypes.data
+            meas[w].n_f = len(f_idx)
+            meas[w].indices_f_to_unique = f_idx.ctypes.data_as(C.POINTER(C.c_int32))
+            meas[w].p_incident = p_in.ctypes.data
+            meas[w].n_mixes = len(mixes_in)
+            meas[w].mixes = mixes
+        d.n_measurements = len(measurements)
+        d.measurements = meas
+        d.device = int(device)
+        _check(lib.cui_born_plan_create(C.byref(d), int(max_objects), C.byref(self._plan)))
+        self.max_objects = int(max_objects)
+        info = BornInfo()
+        _check(lib.cui_born_plan_info(self._plan, C.byref(info)))
+        self.info = {n: int(getattr(info, n)) for n, _ in BornInfo._fields_}
+        self.n_observations = self.info["n_observations"]
+        self.n_points = self.info["n_points"]
+        self.device = int(device)
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_plan", None) and self._plan.value:
+            self._lib.cui_born_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def size(self):
+        """Operator size ``(N_observations, N_points)`` (``operator.m:1042-1045``)."""
+        return self.n_observations, self.n_points
+
+    # ------------------------------------------------------------------ host (FP64)
+    def _host_apply(self, mode: int, x: np.ndarray) -> np.ndarray:
+        x = np.asarray(x)
+        vec = x.ndim == 1
+        x2 = _c128_f(x[:, None] if vec else x)
+        rows_out = self.n_observations if mode == 1 else self.n_points
+        out = np.zeros((rows_out, x2.shape[1]), dtype=np.complex128, order="F")
+        _check(self._lib.cui_born_combined_host(self._plan, mode, x2.ctypes.data, x2.shape[0], x2.shape[1],
+                                                out.ctypes.data, rows_out))
+        return out[:, 0] if vec else out
+
+    # ------------------------------------------------------------------ device (FP32)
+    @staticmethod
+    def _cols(t):
+        """(rows, B) column-major view of a CUDA complex64 tensor as a (B, rows) contiguous tensor."""
+        import torch
+        if t.dtype != torch.complex64 or not t.is_cuda:
+            raise TypeError("device applies take CUDA complex64 tensors")
+        vec = t.dim() == 1
+        tt = t[:, None] if vec else t
+        return tt.t().contiguous(), vec
+
+    def _dev_apply(self, mode: int, x):
+        import torch
+        xc, vec = self._cols(x)
+        B, rows_in = xc.shape
+        rows_out = self.n_observations if mode == 1 else self.n_points
+        out = torch.empty((B, rows_out), dtype=torch.complex64, device=x.device)
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        fn = self._lib.cui_born_forward if mode == 1 else self._lib.cui_born_adjoint
+        _check(fn(self._plan, xc.data_ptr(), rows_in, B, out.data_ptr(), rows_out, stream))
+        out = out.t()
+        return out[:, 0] if vec else out
+
+    def _is_torch(self, x):
+        try:
+            import torch
+        except ImportError:
+            return False
+        return isinstance(x, torch.Tensor)
+
+    def forward(self, gamma):
+        """``u = Phi * gamma`` (``operator_born.m:37-44``)."""
+        return self._dev_apply(1, gamma) if self._is_torch(gamma) else self._host_apply(1, gamma)
+
+    def adjoint(self, u):
+        """``gamma_hat = Phi^H * u`` (``operator_born.m:243-320``)."""
+        return self._dev_apply(2, u) if self._is_torch(u) else self._host_apply(2, u)
+
+    __mul__ = forward
+
+    def combined_scalar(self, mode: int, x=None):
+        """``operator.combined_scalar`` (``operator.m:1019-1072``): 0 size, 1 forward, 2 adjoint."""
+        if mode == 0:
+            return self.size
+        if mode == 1:
+            return self.forward(x)
+        if mode == 2:
+            return self.adjoint(x)
+        raise CuiError(1, "mode must be 0, 1 or 2")
+
+    def vjp(self, gamma, u_meas):
+        """Gradient and value of ``0.5*||Phi gamma - u||^2`` per column: ``(grad, loss)``."""
+        if self._is_torch(gamma):
+            import torch
+            gc, vec = self._cols(gamma)
+            uc, _ = self._cols(u_meas)
+            B = gc.shape[0]
+            grad = torch.empty_like(gc)
+            loss = torch.empty(B, dtype=torch.float32, device=gamma.device)
+            stream = torch.cuda.current_stream(gamma.device).cuda_stream
+            _check(self._lib.cui_born_vjp(self._plan, gc.data_ptr(), self.n_points, uc.data_ptr(),
+                                          self.n_observations, B, grad.data_ptr(), self.n_points,
+                                          loss.data_ptr(), stream))
+            grad = grad.t()
+            return (grad[:, 0], loss[0]) if vec else (grad, loss)
+        g = np.asarray(gamma)
+        vec = g.ndim == 1
+        g2 = _c128_f(g[:, None] if vec else g)
+        u2 = _c128_f(np.asarray(u_meas)[:, None] if vec else u_meas)
+        B = g2.shape[1]
+        grad = np.zeros((self.n_points, B), dtype=np.complex128, order="F")
+        loss = np.zeros(B, dtype=np.float64)
+        _check(self._lib.cui_born_vjp_host(self._plan, g2.ctypes.data, g2.shape[0], u2.ctypes.data, u2.shape[0],
+                                           B, grad.ctypes.data, self.n_points,
+                                           loss.ctypes.data_as(C.POINTER(C.c_double))))
+        return (grad[:, 0], loss[0]) if vec else (grad, loss)
+
+
+def _autograd():
+    import torch
+
+    class BornForward(torch.autograd.Function):
+        """``u = Phi gamma`` with the hand-written adjoint as its backward.
+
+        For the linear map ``Phi`` PyTorch's complex convention gives the
+        input gradient ``Phi^H * grad_u``, which is exactly
+        ``cui_born_adjoint``.
+        """
+
+        @staticmethod
+        def forward(ctx, gamma, op: OperatorBorn):
+            ctx.op = op
+            return op.forward(gamma)
+
+        @staticmethod
+        def backward(ctx, grad_u):
+            return ctx.op.adjoint(grad_u.contiguous()), None
+
+    return BornForward
+
+
+try:  # torch is plumbing for device memory and autograd, not a requirement of the C-ABI
+    BornForward = _autograd()
+except ImportError:  # pragma: no cover
+    BornForward = None
+
+
+def born_forward(gamma, op: OperatorBorn):
+    """Differentiable forward apply (``torch.autograd``)."""
+    return BornForward.apply(gamma, op)

@@ -1,0 +1,132 @@
+// Host-buffer entry points with the MEX gateway's semantics.
+//
+// combined_quick_gpu converts its FP64 input to FP32 on the host, uploads
+// it, runs the operator and converts the FP32 result back to FP64
+// (+scattering/combined_quick_gpu.cu:700-780, :940-1006).  These entry points
+// do the same around the device applies, with pinned staging buffers that
+// the plan allocates on first use and keeps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cui_internal.cuh"
+
+namespace cui {
+namespace {
+
+cui_status ensure_stage(Plan& p) {
+    if (p.h_stage_in) return CUI_OK;
+    const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_in), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_out), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    void* v = nullptr;
+    for (float2** d : {&p.d_stage_in, &p.d_stage_out, &p.d_stage_aux}) {
+        if ((e = cudaMalloc(&v, n * sizeof(float2))) != cudaSuccess) return check_cuda(e, "cudaMalloc");
+        p.allocations.push_back(v);
+        *d = static_cast<float2*>(v);
+    }
+    if ((e = cudaMalloc(&v, sizeof(float) * p.max_objects)) != cudaSuccess) return check_cuda(e, "cudaMalloc");
+    p.allocations.push_back(v);
+    p.d_stage_loss = static_cast<float*>(v);
+    p.h_stage_elems = n;
+    return CUI_OK;
+}
+
+void pack(const cui_complex64* src, int64_t ld, int64_t rows, int B, float2* dst) {
+    for (int b = 0; b < B; ++b)
+        for (int64_t i = 0; i < rows; ++i) {
+            const cui_complex64 c = src[b * ld + i];
+            dst[b * rows + i] = make_float2(static_cast<float>(c.re), static_cast<float>(c.im));
+        }
+}
+
+void unpack(const float2* src, int64_t rows, int B, cui_complex64* dst, int64_t ld) {
+    for (int b = 0; b < B; ++b)
+        for (int64_t i = 0; i < rows; ++i) {
+            const float2 v = src[b * rows + i];
+            dst[b * ld + i].re = v.x;
+            dst[b * ld + i].im = v.y;
+        }
+}
+
+}  // namespace
+}  // namespace cui
+
+extern "C" {
+
+cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_complex64* input, int64_t ld_in,
+                                  int32_t n_objects, cui_complex64* output, int64_t ld_out) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    Plan& p = plan->p;
+    if (mode != 1 && mode != 2)
+        return set_error(CUI_ERR_INVALID_ARG, "mode must be 1 (forward) or 2 (adjoint) (combined_quick_gpu:NoNumericScalarMode)");
+    const int64_t rows_in = (mode == 1) ? p.P : p.n_obs;
+    const int64_t rows_out = (mode == 1) ? p.n_obs : p.P;
+    if (!input || !output || n_objects < 1 || n_objects > p.max_objects || ld_in < rows_in || ld_out < rows_out)
+        return set_error(CUI_ERR_INVALID_ARG, "input must be a matrix with the operator's number of rows "
+                                              "(combined_quick_gpu:NoValidDoubleMatrix)");
+    cudaError_t e = cudaSetDevice(p.device);
+    if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    cui_status s = ensure_stage(p);
+    if (s != CUI_OK) return s;
+    pack(input, ld_in, rows_in, n_objects, p.h_stage_in);
+    const size_t bytes_in = sizeof(float2) * rows_in * n_objects;
+    const size_t bytes_out = sizeof(float2) * rows_out * n_objects;
+    if ((e = cudaMemcpyAsync(p.d_stage_in, p.h_stage_in, bytes_in, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
+        return check_cuda(e, "upload");
+    s = (mode == 1) ? forward_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0)
+                    : adjoint_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0);
+    if (s != CUI_OK) return s;
+    if ((e = cudaMemcpyAsync(p.h_stage_out, p.d_stage_out, bytes_out, cudaMemcpyDeviceToHost, 0)) != cudaSuccess)
+        return check_cuda(e, "download");
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return check_cuda(e, "synchronize");
+    unpack(p.h_stage_out, rows_out, n_objects, output, ld_out);
+    return CUI_OK;
+}
+
+cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, int64_t ld_gamma,
+                             const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects, cui_complex64* grad,
+                             int64_t ld_grad, double* loss) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    Plan& p = plan->p;
+    if (!gamma || !u_meas || !grad || n_objects < 1 || n_objects > p.max_objects || ld_gamma < p.P ||
+        ld_u < p.n_obs || ld_grad < p.P)
+        return set_error(CUI_ERR_INVALID_ARG, "invalid arguments to cui_born_vjp_host");
+    cudaError_t e = cudaSetDevice(p.device);
+    if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    cui_status s = ensure_stage(p);
+    if (s != CUI_OK) return s;
+    // gamma and u_meas share the input staging buffer: gamma first, then u_meas
+    const int64_t ng = p.P * n_objects, nu = p.n_obs * n_objects;
+    if (static_cast<size_t>(ng) > p.h_stage_elems || static_cast<size_t>(nu) > p.h_stage_elems)
+        return set_error(CUI_ERR_INVALID_ARG, "staging buffer too small");
+    pack(gamma, ld_gamma, p.P, n_objects, p.h_stage_in);
+    if ((e = cudaMemcpyAsync(p.d_stage_in, p.h_stage_in, sizeof(float2) * ng, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
+        return check_cuda(e, "upload gamma");
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return check_cuda(e, "synchronize");
+    pack(u_meas, ld_u, p.n_obs, n_objects, p.h_stage_in);
+    if ((e = cudaMemcpyAsync(p.d_stage_aux, p.h_stage_in, sizeof(float2) * nu, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
+        return check_cuda(e, "upload u");
+    s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0);
+    if (s != CUI_OK) return s;
+    if ((e = cudaMemcpyAsync(p.h_stage_out, p.d_stage_out, sizeof(float2) * ng, cudaMemcpyDeviceToHost, 0)) != cudaSuccess)
+        return check_cuda(e, "download");
+    std::vector<float> hl(n_objects);
+    if (loss && (e = cudaMemcpyAsync(hl.data(), p.d_stage_loss, sizeof(float) * n_objects, cudaMemcpyDeviceToHost, 0)) !=
+                    cudaSuccess)
+        return check_cuda(e, "download loss");
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return check_cuda(e, "synchronize");
+    unpack(p.h_stage_out, p.P, n_objects, grad, ld_grad);
+    if (loss)
+        for (int b = 0; b < n_objects; ++b) loss[b] = hl[b];
+    return CUI_OK;
+}
+
+}  // extern "C"

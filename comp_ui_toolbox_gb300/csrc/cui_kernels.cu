@@ -1,0 +1,666 @@
+// FP32 Born operator kernels for sm_103a and the device apply entry points.
+//
+// The reference builds the matrix Phi_e = h_e .* p_in .* pref_e for every
+// (measurement, mix, active element), writes it to global memory and hands
+// it to cuBLAS (+scattering/combined_quick_gpu.cu:1099-1124, :902-921).  Here
+// the element sum is taken out of the mixing:
+//
+//   forward   G[s, e]  = sum_p  h(f_s; o(p, e), z_p) * p_in[s, p] * gamma[p]
+//             u[row]   = sum_{a in mix} pref[mix, f_row, a] * G[s_row, act[a]]
+//   adjoint   V[s, e]  = sum_{rows of s} conj(pref[mix, f_row, pos(e)]) * u[row]
+//             gh[p]    = sum_s conj(p_in[s, p]) * sum_e conj(h(f_s; o(p, e), z_p)) * V[s, e]
+//
+// with o(p, e) = i_x - e_x*ppp_x + (E_x-1)*ppp_x (and likewise in y) the
+// signed lateral offset that indexes the lateral table.  Along one grid line
+// (fixed z, y) and one residue r = i_x mod ppp_x the table entries form a
+// Toeplitz band: h(r + ppp*j, e) = A_r[j - e + E_x - 1].  Each thread keeps a
+// register window of KE (forward) or KJ (adjoint) consecutive band entries
+// and slides it by one entry per step, so a step costs one shared-memory load
+// of the band plus broadcast loads of the wave columns.  Table rows and
+// incident-field rows are staged in shared memory per grid line; partial sums
+// go to plan-owned scratch and are reduced in a fixed order (deterministic).
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <algorithm>
+
+#include "cui_internal.cuh"
+
+namespace cui {
+
+namespace {
+
+constexpr int kPad = 8;  // zero padding on both ends of each staged band
+
+__device__ __forceinline__ void cmac(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+}
+
+// acc += conj(a) * b
+__device__ __forceinline__ void cmac_conj(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+struct LineGeom {
+    int Nx, Ny, Nz, Ex, Ey, ppx, ppy, Nox, Noy;
+    int64_t P;
+    int E, S, F;
+    int Ni, Nj_max;
+};
+
+// Stage table row (f, z, oy) into residue-major bands: band r holds
+// A_r[i] = row[r + ppx*i] at sA[r*Ni + kPad + i]; entries outside the row are 0.
+__device__ __forceinline__ void stage_band(float2* sA, const float2* __restrict__ row, const LineGeom& g) {
+    const int n = g.ppx * g.Ni;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int r = idx / g.Ni;
+        const int i = idx - r * g.Ni - kPad;
+        const int o = r + g.ppx * i;
+        sA[idx] = (i >= 0 && o < g.Nox) ? __ldg(row + o) : make_float2(0.f, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dense forward: block = (line group x ey, frequency, object x column pass)
+// ---------------------------------------------------------------------------
+struct FwdArgs {
+    LineGeom g;
+    const float2* __restrict__ table;
+    const float2* __restrict__ p_in;
+    const float2* __restrict__ gamma;
+    int64_t ldg;
+    const int* __restrict__ f_slot_ptr;
+    const int* __restrict__ f_slot_list;
+    int lines_per_group, n_lines;
+    int n_eg, nseg, Js, ntask;
+    int B, npass;
+    float2* __restrict__ part;  // [groups][S][B][E]
+};
+
+template <int NC, int KE>
+__global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
+    extern __shared__ float4 smem_f4[];
+    const LineGeom& g = a.g;
+    float2* sA = reinterpret_cast<float2*>(smem_f4);
+    float2* sQ = sA + g.ppx * g.Ni;          // [Nx][NC]
+    float2* sR = sQ + g.Nx * NC;             // [Ex][NC]
+    __shared__ int sSlot[NC];
+
+    const int grp = blockIdx.x / g.Ey, ey = blockIdx.x - grp * g.Ey;
+    const int f = blockIdx.y;
+    const int b = blockIdx.z / a.npass, cp = blockIdx.z - b * a.npass;
+    const int s0 = a.f_slot_ptr[f];
+    const int ns = a.f_slot_ptr[f + 1] - s0;
+    const int c0 = cp * NC;
+    if (c0 >= ns) return;  // uniform over the block
+    const int nc = min(NC, ns - c0);
+    if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool task_on = warp < a.ntask;
+    int r = 0, eg = 0, seg = 0;
+    if (task_on) {
+        r = warp % g.ppx;
+        const int rest = warp / g.ppx;
+        eg = rest % a.n_eg;
+        seg = rest / a.n_eg;
+    }
+    const int e0 = (eg * 32 + lane) * KE;
+    const int Nj_r = (r < g.Nx) ? (g.Nx - r + g.ppx - 1) / g.ppx : 0;
+    const int jlo = seg * a.Js, jhi = min(jlo + a.Js, Nj_r);
+    const bool lane_on = task_on && (e0 < g.Ex) && (jlo < jhi);
+
+    float2 acc[KE][NC];
+#pragma unroll
+    for (int t = 0; t < KE; ++t)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[t][c] = make_float2(0.f, 0.f);
+
+    const int line0 = grp * a.lines_per_group;
+    const int line1 = min(line0 + a.lines_per_group, a.n_lines);
+    for (int line = line0; line < line1; ++line) {
+        const int iy = line % g.Ny, z = line / g.Ny;
+        const int oy = iy - ey * g.ppy + (g.Ey - 1) * g.ppy;
+        const float2* trow = a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox;
+        const int64_t pt0 = (static_cast<int64_t>(z) * g.Ny + iy) * g.Nx;
+        __syncthreads();
+        stage_band(sA, trow, g);
+        const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg + pt0;
+        for (int idx = threadIdx.x; idx < NC * g.Nx; idx += blockDim.x) {
+            const int c = idx / g.Nx, x = idx - c * g.Nx;
+            float2 q = make_float2(0.f, 0.f);
+            if (c < nc) q = cmul(__ldg(a.p_in + static_cast<int64_t>(sSlot[c]) * g.P + pt0 + x), __ldg(gam + x));
+            sQ[x * NC + c] = q;
+        }
+        __syncthreads();
+        if (lane_on) {
+            const float2* Ar = sA + r * g.Ni + kPad;
+            int base = jlo - e0 + g.Ex - 1;
+            float2 win[KE];
+#pragma unroll
+            for (int t = 0; t < KE; ++t) win[t] = Ar[base - t];
+            for (int j = jlo; j < jhi; ++j) {
+                const float2* qx = sQ + (r + g.ppx * j) * NC;
+                float2 q[NC];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) q[c] = qx[c];
+#pragma unroll
+                for (int t = 0; t < KE; ++t)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) cmac(acc[t][c], win[t], q[c]);
+#pragma unroll
+                for (int t = KE - 1; t > 0; --t) win[t] = win[t - 1];
+                ++base;
+                win[0] = Ar[base];
+            }
+        }
+    }
+
+    // deterministic reduction over (residue, segment) tasks of the block
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < g.Ex * NC; idx += blockDim.x) sR[idx] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int w = 0; w < a.ntask; ++w) {
+        if (warp == w && lane_on) {
+#pragma unroll
+            for (int t = 0; t < KE; ++t) {
+                const int e = e0 + t;
+                if (e < g.Ex) {
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        float2 v = sR[e * NC + c];
+                        v.x += acc[t][c].x;
+                        v.y += acc[t][c].y;
+                        sR[e * NC + c] = v;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < nc * g.Ex; idx += blockDim.x) {
+        const int c = idx / g.Ex, ex = idx - c * g.Ex;
+        const int64_t o = ((static_cast<int64_t>(grp) * g.S + sSlot[c]) * a.B + b) * g.E + ex + g.Ex * ey;
+        a.part[o] = sR[ex * NC + c];
+    }
+}
+
+// G[s][b][e] = sum over line groups of the forward partials
+__global__ void reduce_groups_kernel(const float2* __restrict__ part, int groups, int64_t n, float2* __restrict__ G) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int k = 0; k < groups; ++k) {
+            const float2 v = part[k * n + i];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        G[i] = s;
+    }
+}
+
+// u[b][row] = sum_a pref[mix, fl, a] * G[slot][b][act[a]]  (one warp per (row, b))
+struct MixArgs {
+    const float2* __restrict__ G;
+    const int* __restrict__ row_slot;
+    const int* __restrict__ row_mix;
+    const int* __restrict__ row_fl;
+    const int* __restrict__ mix_nact;
+    const int* __restrict__ mix_nf;
+    const int64_t* __restrict__ mix_pref_off;
+    const int* __restrict__ mix_act_off;
+    const int* __restrict__ act;
+    const float2* __restrict__ pref;
+    int64_t n_obs;
+    int B, E;
+    float2* __restrict__ u;
+    int64_t ldu;
+};
+
+__global__ void mix_kernel(const MixArgs a) {
+    const int64_t wid = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= a.n_obs * a.B) return;
+    const int64_t row = wid % a.n_obs;
+    const int b = static_cast<int>(wid / a.n_obs);
+    const int m = a.row_mix[row], fl = a.row_fl[row], s = a.row_slot[row];
+    const int nact = a.mix_nact[m], nf = a.mix_nf[m];
+    const float2* pr = a.pref + a.mix_pref_off[m] + fl;
+    const int* ac = a.act + a.mix_act_off[m];
+    const float2* Gs = a.G + (static_cast<int64_t>(s) * a.B + b) * a.E;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = lane; k < nact; k += 32) cmac(acc, pr[static_cast<int64_t>(k) * nf], Gs[ac[k]]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, off);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, off);
+    }
+    if (lane == 0) a.u[b * a.ldu + row] = acc;
+}
+
+// V[s][b][e] = sum_{rows of s} conj(pref[mix, fl, pos(e)]) * u[b][row]
+struct UnmixArgs {
+    const float2* __restrict__ u;
+    int64_t ldu;
+    const int* __restrict__ slot_row_ptr;
+    const int* __restrict__ slot_rows;
+    const int* __restrict__ row_mix;
+    const int* __restrict__ row_fl;
+    const int* __restrict__ mix_nf;
+    const int64_t* __restrict__ mix_pref_off;
+    const int* __restrict__ pos;
+    const float2* __restrict__ pref;
+    int S, B, E;
+    float2* __restrict__ V;
+};
+
+__global__ void unmix_kernel(const UnmixArgs a) {
+    const int64_t n = static_cast<int64_t>(a.S) * a.B * a.E;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int e = static_cast<int>(i % a.E);
+        const int64_t sb = i / a.E;
+        const int b = static_cast<int>(sb % a.B);
+        const int s = static_cast<int>(sb / a.B);
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = a.slot_row_ptr[s]; k < a.slot_row_ptr[s + 1]; ++k) {
+            const int row = a.slot_rows[k];
+            const int m = a.row_mix[row];
+            const int ps = a.pos[static_cast<int64_t>(m) * a.E + e];
+            if (ps >= 0) {
+                const float2 p = a.pref[a.mix_pref_off[m] + a.row_fl[row] + static_cast<int64_t>(ps) * a.mix_nf[m]];
+                cmac_conj(acc, p, a.u[b * a.ldu + row]);
+            }
+        }
+        a.V[i] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dense adjoint: block = (grid line, frequency chunk, object)
+// ---------------------------------------------------------------------------
+struct AdjArgs {
+    LineGeom g;
+    const float2* __restrict__ table;
+    const float2* __restrict__ p_in;
+    const float2* __restrict__ V;   // [S][B][E]
+    const int* __restrict__ f_slot_ptr;
+    const int* __restrict__ f_slot_list;
+    int fchunk;
+    int n_jg, nseg_e, Es, ntask;
+    int B;
+    float2* __restrict__ part;      // [nfc][B][P]
+};
+
+template <int NC, int KJ>
+__global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
+    extern __shared__ float4 smem_f4[];
+    const LineGeom& g = a.g;
+    float2* sA = reinterpret_cast<float2*>(smem_f4);
+    float2* sV = sA + g.ppx * g.Ni;   // [Ex][NC]
+    float2* sR = sV + g.Ex * NC;      // [Nx]
+    __shared__ int sSlot[NC];
+
+    const int line = blockIdx.x;
+    const int iy = line % g.Ny, z = line / g.Ny;
+    const int fc = blockIdx.y, b = blockIdx.z;
+    const int64_t pt0 = (static_cast<int64_t>(z) * g.Ny + iy) * g.Nx;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool task_on = warp < a.ntask;
+    int r = 0, jg = 0, es = 0;
+    if (task_on) {
+        r = warp % g.ppx;
+        const int rest = warp / g.ppx;
+        jg = rest % a.n_jg;
+        es = rest / a.n_jg;
+    }
+    const int j0 = (jg * 32 + lane) * KJ;
+    const int Nj_r = (r < g.Nx) ? (g.Nx - r + g.ppx - 1) / g.ppx : 0;
+    const int elo = es * a.Es, ehi = min(elo + a.Es, g.Ex);
+    const bool lane_on = task_on && (j0 < Nj_r) && (elo < ehi);
+
+    float2 gacc[KJ];
+#pragma unroll
+    for (int t = 0; t < KJ; ++t) gacc[t] = make_float2(0.f, 0.f);
+
+    const int f_lo = fc * a.fchunk, f_hi = min(f_lo + a.fchunk, g.F);
+    for (int f = f_lo; f < f_hi; ++f) {
+        const int s0 = a.f_slot_ptr[f];
+        const int ns = a.f_slot_ptr[f + 1] - s0;
+        for (int c0 = 0; c0 < ns; c0 += NC) {
+            const int nc = min(NC, ns - c0);
+            float2 Z[KJ][NC];
+#pragma unroll
+            for (int t = 0; t < KJ; ++t)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) Z[t][c] = make_float2(0.f, 0.f);
+            for (int ey = 0; ey < g.Ey; ++ey) {
+                const int oy = iy - ey * g.ppy + (g.Ey - 1) * g.ppy;
+                const float2* trow = a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox;
+                __syncthreads();
+                if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
+                stage_band(sA, trow, g);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < NC * g.Ex; idx += blockDim.x) {
+                    const int c = idx / g.Ex, ex = idx - c * g.Ex;
+                    sV[ex * NC + c] = (c < nc)
+                        ? __ldg(a.V + (static_cast<int64_t>(sSlot[c]) * a.B + b) * g.E + ex + g.Ex * ey)
+                        : make_float2(0.f, 0.f);
+                }
+                __syncthreads();
+                if (lane_on) {
+                    const float2* Ar = sA + r * g.Ni + kPad;
+                    int base = j0 - elo + g.Ex - 1;
+                    float2 win[KJ];
+#pragma unroll
+                    for (int t = 0; t < KJ; ++t) win[t] = Ar[base + t];
+                    for (int e = elo; e < ehi; ++e) {
+                        const float2* vx = sV + e * NC;
+                        float2 v[NC];
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) v[c] = vx[c];
+#pragma unroll
+                        for (int t = 0; t < KJ; ++t)
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) cmac_conj(Z[t][c], win[t], v[c]);
+#pragma unroll
+                        for (int t = KJ - 1; t > 0; --t) win[t] = win[t - 1];
+                        --base;
+                        win[0] = Ar[base];
+                    }
+                }
+            }
+            if (lane_on) {
+#pragma unroll
+                for (int t = 0; t < KJ; ++t) {
+                    const int x = r + g.ppx * (j0 + t);
+                    if (x < g.Nx) {
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) {
+                            if (c < nc) {
+                                const float2 p = __ldg(a.p_in + static_cast<int64_t>(sSlot[c]) * g.P + pt0 + x);
+                                cmac_conj(gacc[t], p, Z[t][c]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // deterministic reduction over element segments
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < g.Nx; idx += blockDim.x) sR[idx] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int w = 0; w < a.ntask; ++w) {
+        if (warp == w && lane_on) {
+#pragma unroll
+            for (int t = 0; t < KJ; ++t) {
+                const int x = r + g.ppx * (j0 + t);
+                if (x < g.Nx) {
+                    float2 v = sR[x];
+                    v.x += gacc[t].x;
+                    v.y += gacc[t].y;
+                    sR[x] = v;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    float2* out = a.part + (static_cast<int64_t>(fc) * a.B + b) * g.P + pt0;
+    for (int x = threadIdx.x; x < g.Nx; x += blockDim.x) out[x] = sR[x];
+}
+
+// gamma_hat[b][p] = sum over frequency chunks
+__global__ void reduce_fchunks_kernel(const float2* __restrict__ part, int nfc, int B, int64_t P,
+                                      float2* __restrict__ out, int64_t ldo) {
+    const int64_t n = static_cast<int64_t>(B) * P;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int k = 0; k < nfc; ++k) {
+            const float2 v = part[k * n + i];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        const int64_t b = i / P, p = i - b * P;
+        out[b * ldo + p] = s;
+    }
+}
+
+// r = u_pred - u_meas in place; per-block partial sums of 0.5*|r|^2
+constexpr int kLossBlocks = 128;
+
+__global__ void residual_kernel(float2* __restrict__ r, int64_t ldr, const float2* __restrict__ um, int64_t ldu,
+                                int64_t n_obs, float* __restrict__ loss_part) {
+    const int b = blockIdx.y;
+    float s = 0.f;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n_obs;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float2 v = r[b * ldr + i];
+        const float2 w = um[b * ldu + i];
+        v.x -= w.x;
+        v.y -= w.y;
+        r[b * ldr + i] = v;
+        s = fmaf(v.x, v.x, s);
+        s = fmaf(v.y, v.y, s);
+    }
+    __shared__ float red[32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if (threadIdx.x == 0) loss_part[b * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void loss_final_kernel(const float* __restrict__ part, int nblk, int B, float* __restrict__ loss) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    float s = 0.f;
+    for (int k = 0; k < nblk; ++k) s += part[b * nblk + k];
+    loss[b] = 0.5f * s;
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+LineGeom geom_of(const Plan* p) {
+    LineGeom g;
+    g.Nx = p->Nx; g.Ny = p->Ny; g.Nz = p->Nz; g.Ex = p->Ex; g.Ey = p->Ey;
+    g.ppx = p->ppx; g.ppy = p->ppy; g.Nox = p->Nox; g.Noy = p->Noy;
+    g.P = p->P; g.E = p->E; g.S = p->S; g.F = p->F; g.Ni = p->Ni; g.Nj_max = p->Nj_max;
+    return g;
+}
+
+int pick_nc(int slots) {
+    if (slots <= 1) return 1;
+    if (slots <= 2) return 2;
+    if (slots <= 4) return 4;
+    if (slots <= 8) return 8;
+    if (slots <= 12) return 12;
+    return 16;
+}
+
+constexpr int fwd_ke(int nc) { return nc >= 16 ? 2 : 4; }
+constexpr int adj_kj(int nc) { return nc >= 12 ? 2 : 4; }
+
+struct FwdShape { int n_eg, nseg, Js, ntask, threads; };
+struct AdjShape { int n_jg, nseg_e, Es, ntask, threads; };
+
+FwdShape fwd_shape(const Plan* p, int ke) {
+    FwdShape s;
+    s.n_eg = (p->Ex + 32 * ke - 1) / (32 * ke);
+    const int base = p->ppx * s.n_eg;
+    s.nseg = std::max(1, 8 / base);
+    s.nseg = std::min(s.nseg, std::max(1, p->Nj_max));
+    s.Js = (p->Nj_max + s.nseg - 1) / s.nseg;
+    s.ntask = base * s.nseg;
+    s.threads = 32 * s.ntask;
+    return s;
+}
+
+AdjShape adj_shape(const Plan* p, int kj) {
+    AdjShape s;
+    s.n_jg = (p->Nj_max + 32 * kj - 1) / (32 * kj);
+    const int base = p->ppx * s.n_jg;
+    s.nseg_e = std::max(1, 8 / base);
+    s.nseg_e = std::min(s.nseg_e, p->Ex);
+    s.Es = (p->Ex + s.nseg_e - 1) / s.nseg_e;
+    s.ntask = base * s.nseg_e;
+    s.threads = 32 * s.ntask;
+    return s;
+}
+
+template <int NC>
+cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
+    constexpr int KE = fwd_ke(NC);
+    const FwdShape sh = fwd_shape(p, KE);
+    FwdArgs a;
+    a.g = geom_of(p);
+    a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.lines_per_group = p->fwd_lines_per_group; a.n_lines = p->Ny * p->Nz;
+    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask;
+    a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
+    a.part = p->ws_part;
+    const size_t smem = fwd_smem_bytes(p, NC);
+    cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(p->fwd_groups * p->Ey, p->F, B * a.npass);
+    fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int NC>
+cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
+    constexpr int KJ = adj_kj(NC);
+    const AdjShape sh = adj_shape(p, KJ);
+    AdjArgs a;
+    a.g = geom_of(p);
+    a.table = p->table; a.p_in = p->p_in; a.V = p->ws_G;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.fchunk = p->adj_fchunk;
+    a.n_jg = sh.n_jg; a.nseg_e = sh.nseg_e; a.Es = sh.Es; a.ntask = sh.ntask;
+    a.B = B; a.part = p->ws_part;
+    const size_t smem = adj_smem_bytes(p, NC);
+    cudaError_t e = cudaFuncSetAttribute(adj_dense_kernel<NC, KJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(p->Ny * p->Nz, p->adj_nfc, B);
+    adj_dense_kernel<NC, KJ><<<grid, sh.threads, smem, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+int grid_1d(int64_t n, int threads) {
+    const int64_t b = (n + threads - 1) / threads;
+    return static_cast<int>(std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32));
+}
+
+cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
+    cudaError_t e;
+    switch (pick_nc(p->max_slots_per_f)) {
+        case 1: e = launch_fwd<1>(p, gamma, ldg, B, st); break;
+        case 2: e = launch_fwd<2>(p, gamma, ldg, B, st); break;
+        case 4: e = launch_fwd<4>(p, gamma, ldg, B, st); break;
+        case 8: e = launch_fwd<8>(p, gamma, ldg, B, st); break;
+        case 12: e = launch_fwd<12>(p, gamma, ldg, B, st); break;
+        default: e = launch_fwd<16>(p, gamma, ldg, B, st); break;
+    }
+    if (e != cudaSuccess) return e;
+    const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
+    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, p->fwd_groups, n, p->ws_G);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    MixArgs m;
+    m.G = p->ws_G; m.row_slot = p->row_slot; m.row_mix = p->row_mix; m.row_fl = p->row_fl;
+    m.mix_nact = p->mix_nact; m.mix_nf = p->mix_nf; m.mix_pref_off = p->mix_pref_off; m.mix_act_off = p->mix_act_off;
+    m.act = p->act; m.pref = p->pref; m.n_obs = p->n_obs; m.B = B; m.E = p->E; m.u = u; m.ldu = ldu;
+    const int64_t warps = p->n_obs * B;
+    const int64_t blocks = (warps * 32 + 255) / 256;
+    mix_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(m);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st) {
+    UnmixArgs a;
+    a.u = u; a.ldu = ldu; a.slot_row_ptr = p->slot_row_ptr; a.slot_rows = p->slot_rows;
+    a.row_mix = p->row_mix; a.row_fl = p->row_fl; a.mix_nf = p->mix_nf; a.mix_pref_off = p->mix_pref_off;
+    a.pos = p->pos; a.pref = p->pref; a.S = p->S; a.B = B; a.E = p->E; a.V = p->ws_G;
+    const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
+    unmix_kernel<<<grid_1d(n, 256), 256, 0, st>>>(a);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    switch (pick_nc(p->max_slots_per_f)) {
+        case 1: e = launch_adj<1>(p, B, st); break;
+        case 2: e = launch_adj<2>(p, B, st); break;
+        case 4: e = launch_adj<4>(p, B, st); break;
+        case 8: e = launch_adj<8>(p, B, st); break;
+        case 12: e = launch_adj<12>(p, B, st); break;
+        default: e = launch_adj<16>(p, B, st); break;
+    }
+    if (e != cudaSuccess) return e;
+    const int64_t m = static_cast<int64_t>(B) * p->P;
+    reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, p->adj_nfc, B, p->P, g, ldg);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t fwd_smem_bytes(const Plan* p, int nc) {
+    return sizeof(float2) * (static_cast<size_t>(p->ppx) * p->Ni + static_cast<size_t>(p->Nx) * nc +
+                             static_cast<size_t>(p->Ex) * nc);
+}
+
+size_t adj_smem_bytes(const Plan* p, int nc) {
+    return sizeof(float2) * (static_cast<size_t>(p->ppx) * p->Ni + static_cast<size_t>(p->Ex) * nc +
+                             static_cast<size_t>(p->Nx));
+}
+
+cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
+    return check_cuda(run_forward(p, gamma, ldg, B, u, ldu, st), "forward");
+}
+
+cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st) {
+    return check_cuda(run_adjoint(p, u, ldu, B, g, ldg, st), "adjoint");
+}
+
+cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
+                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st) {
+    cudaError_t e = run_forward(p, gamma, ldg, B, p->ws_r, p->n_obs, st);
+    if (e != cudaSuccess) return check_cuda(e, "vjp forward");
+    residual_kernel<<<dim3(kLossBlocks, B), 256, 0, st>>>(p->ws_r, p->n_obs, um, ldu, p->n_obs, p->ws_loss);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "vjp residual");
+    if (loss != nullptr) {
+        loss_final_kernel<<<(B + 127) / 128, 128, 0, st>>>(p->ws_loss, kLossBlocks, B, loss);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "vjp loss");
+    }
+    return check_cuda(run_adjoint(p, p->ws_r, p->n_obs, B, grad, ldgr, st), "vjp adjoint");
+}
+
+size_t loss_workspace_floats(int max_objects) { return static_cast<size_t>(kLossBlocks) * max_objects; }
+
+}  // namespace cui

@@ -1,0 +1,175 @@
+/*
+ * cui_born.h -- C-ABI of the GB300 Born scattering operator.
+ *
+ * Drop-in for the reference toolbox's MEX path (mschiffn/comp_ui_toolbox):
+ *   output = scattering.combined_quick_gpu( operator_born, mode, input )
+ * (+scattering/combined_quick_gpu.m:11, +scattering/combined_quick_gpu.cu:66-1094),
+ * called from operator_born.forward_scalar / adjoint_scalar
+ * (+scattering/operator_born.m:217, :286).
+ *
+ * The MEX function re-reads every operator table from MATLAB and uploads it
+ * on each call.  Here the tables are uploaded once into a persistent plan
+ * (cui_born_plan_create) and every apply only moves its input and output.
+ *
+ * Conventions
+ *   - complex numbers are interleaved (re, im): cui_complex64 matches
+ *     MATLAB's mxComplexDouble, cui_complex32 matches cuComplex / float2;
+ *   - matrices are column-major with an explicit leading dimension;
+ *   - index arrays copied from MATLAB are 1-based, as MATLAB stores them;
+ *   - `stream` is a cudaStream_t passed as void* (0 = legacy default stream);
+ *   - device applies are asynchronous on `stream`, allocate nothing and do
+ *     not synchronise; one plan serves one stream at a time (its workspace
+ *     is shared by all applies of the plan).
+ *   - no function ever calls cudaDeviceReset (the reference does on any CUDA
+ *     error, +scattering/combined_quick_gpu.h:38-42).
+ */
+#ifndef CUI_BORN_H
+#define CUI_BORN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The MEX shim maps them onto the reference's error IDs
+ * (+scattering/combined_quick_gpu.cu:201, :228, :374, :385, :397, :414,
+ * :421, :428 and combined_quick_gpu.h:43). */
+typedef enum {
+    CUI_OK = 0,
+    CUI_ERR_INVALID_ARG = 1,       /* combined_quick_gpu:NoValidDoubleMatrix, :NumberArguments, :NoNumericScalarMode */
+    CUI_ERR_UNSUPPORTED_SETUP = 2, /* combined_quick_gpu:NoSymmetricGridsSetup (index map is not a lateral shift) */
+    CUI_ERR_OOM = 3,               /* device or host allocation failed */
+    CUI_ERR_CUDA = 4,              /* adjoint_quick_gpu:ErrorCUDA */
+    CUI_ERR_TIMEOUT = 5,           /* a bounded device-side wait gave up */
+    CUI_ERR_NUMERIC = 6,           /* non-finite table entries */
+    CUI_ERR_NO_DEVICE = 7          /* combined_quick_gpu:NoCUDADevices / :InvalidCUDADevice */
+} cui_status;
+
+typedef struct { double re, im; } cui_complex64;
+typedef struct { float re, im; } cui_complex32;
+
+typedef struct cui_born_plan cui_born_plan;
+
+/* One mixed voltage signal of a pulse-echo measurement
+ * (sequence.settings(m).rx(mix), sequence.prefactors{m}(mix)). */
+typedef struct {
+    int32_t n_f;                          /* number of frequencies of the mix */
+    const int32_t* indices_f_to_unique;   /* [n_f] 1-based into the measurement's unique frequencies
+                                             (settings(m).indices_f_to_unique{mix}, read at .cu:313) */
+    int32_t n_active;                     /* number of active elements */
+    const int32_t* indices_active;        /* [n_active] 1-based element indices (rx(mix).indices_active, .cu:309) */
+    const cui_complex64* prefactors;      /* [n_f x n_active] column-major (prefactors{m}(mix).samples.values, .cu:352) */
+} cui_mix_desc;
+
+/* One sequential pulse-echo measurement (incident wave). */
+typedef struct {
+    int32_t n_f;                          /* unique frequencies of the measurement */
+    const int32_t* indices_f_to_unique;   /* [n_f] 1-based into the global unique frequencies
+                                             (sequence.indices_f_to_unique{m}, .cu:278) */
+    const cui_complex64* p_incident;      /* [n_f x N_points] column-major
+                                             (incident_waves(m).p_incident.samples.values, .cu:817-823) */
+    int32_t n_mixes;
+    const cui_mix_desc* mixes;
+} cui_measurement_desc;
+
+typedef enum {
+    /* sequence.h_ref.samples.values [n_f_unique x N_points] plus
+     * setup.indices_grid_FOV_shift [N_points x N_elements] (1-based), exactly
+     * what the MEX reads (.cu:231, :382-391).  The plan checks that the map
+     * is the symmetric-grid lateral shift (setup_grid_symmetric.m:175-232)
+     * and stores the distinct entries as a lateral-offset table. */
+    CUI_TABLE_REFERENCE = 0,
+    /* The lateral-offset table itself: entry (f, z, [o_y,] o_x) is the
+     * transfer function of an element at signed lateral grid offset
+     * i_d - e_d*ppp_d = o_d - (E_d-1)*ppp_d, depth index z; column-major
+     * [No_x x (No_y) x N_z x n_f_unique], No_d = N_d + (E_d-1)*ppp_d. */
+    CUI_TABLE_LATERAL = 1
+} cui_table_form;
+
+/* Everything combined_quick_gpu reads from the operator (.cu:203-393). */
+typedef struct {
+    int32_t n_dims;                 /* 2 or 3 (FOV grid dimensions) */
+    int32_t n_points_axis[3];       /* FOV grid points: lateral axes then axial (FOV.shape.grid.N_points_axis) */
+    int32_t n_elements_axis[2];     /* array elements per lateral axis (xdc_array.N_elements_axis) */
+    int32_t n_points_per_pitch[2];  /* setup.N_points_per_pitch_axis */
+    int32_t n_f_unique;             /* rows of h_ref (.cu:394) */
+    int32_t table_form;             /* cui_table_form */
+    const cui_complex64* h_ref;                 /* CUI_TABLE_REFERENCE */
+    const int32_t* indices_grid_FOV_shift;      /* CUI_TABLE_REFERENCE */
+    const cui_complex64* h_lateral;             /* CUI_TABLE_LATERAL */
+    int32_t n_measurements;         /* selected measurements (indices_measurement_sel, .cu:238) */
+    const cui_measurement_desc* measurements;
+    int32_t device;                 /* CUDA device (options.momentary.gpu.index, .cu:378) */
+} cui_born_desc;
+
+/* Work and storage figures of a plan (bytes and complex multiply-adds). */
+typedef struct {
+    int64_t n_points;               /* N_points */
+    int64_t n_observations;         /* rows of the forward output (sequence.size(1)) */
+    int64_t n_elements;
+    int64_t n_slots;                /* (measurement, unique frequency) pairs */
+    int64_t n_f_unique;
+    int64_t table_bytes;            /* device bytes of the lateral table */
+    int64_t incident_bytes;         /* device bytes of all incident fields */
+    int64_t workspace_bytes;        /* device scratch owned by the plan */
+    int64_t contraction_macs;       /* complex MACs of one dense apply per object: sum_slots E*P */
+} cui_born_info;
+
+/* ---- plan lifetime ------------------------------------------------------ */
+/* Validates the descriptor, converts every table to FP32 in the device
+ * layout and uploads it.  Replaces the per-call host conversion and uploads
+ * of .cu:520-850.  `max_objects` bounds the number of columns of one apply
+ * (it sizes the plan's workspace). */
+cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, cui_born_plan** plan);
+cui_status cui_born_plan_destroy(cui_born_plan* plan);
+cui_status cui_born_plan_info(const cui_born_plan* plan, cui_born_info* info);
+
+/* combined_scalar mode 0 (+scattering/operator.m:1042-1045): operator size. */
+cui_status cui_born_size(const cui_born_plan* plan, int64_t* n_observations, int64_t* n_points);
+
+/* ---- device applies (FP32, device pointers) ------------------------------
+ * Forward, mode 1 (.cu:902-909; operator_born.m:332-470):
+ *   u[:, b] = Phi * gamma[:, b],  gamma: N_points x n_objects, u: N_obs x n_objects.
+ * Rows of u are ordered measurement -> mix -> frequency (.cu:978). */
+cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
+                            int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream);
+
+/* Adjoint, mode 2 (.cu:914-921; operator_born.m:480-596):
+ *   gamma_hat[:, b] = Phi^H * u[:, b]. */
+cui_status cui_born_adjoint(cui_born_plan* plan, const cui_complex32* u, int64_t ld_u,
+                            int32_t n_objects, cui_complex32* gamma_hat, int64_t ld_gamma, void* stream);
+
+/* Vector-Jacobian product of the data-fidelity term used by the
+ * reference's solvers (operator.m:717 -> omp.m:170, spgl1.m:154):
+ *   r = Phi*gamma - u_meas,  loss[b] = 0.5*||r[:, b]||^2,  grad = Phi^H r.
+ * `loss` is a device pointer to n_objects floats (may be NULL). */
+cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
+                        const cui_complex32* u_meas, int64_t ld_u, int32_t n_objects,
+                        cui_complex32* grad, int64_t ld_grad, float* loss, void* stream);
+
+/* ---- host applies (FP64, MEX semantics) ----------------------------------
+ * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
+ * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).
+ * Host buffers in MATLAB's interleaved complex double; FP64 <-> FP32
+ * conversion and host <-> device copies happen inside, synchronously. */
+cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_complex64* input,
+                                  int64_t ld_in, int32_t n_objects, cui_complex64* output, int64_t ld_out);
+
+/* Host VJP: same as cui_born_vjp with host FP64 buffers; loss may be NULL. */
+cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, int64_t ld_gamma,
+                             const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects,
+                             cui_complex64* grad, int64_t ld_grad, double* loss);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+const char* cui_status_string(cui_status status);
+/* Message of the last failing call on this thread (empty if none). */
+const char* cui_last_error(void);
+/* Number of kernel launches issued by this process (all plans). */
+int64_t cui_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUI_BORN_H */

@@ -1,0 +1,12 @@
+"""Shared pytest setup: the ``gpu`` marker and the repo root on sys.path."""
+
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the compiled libcui_born.so")

@@ -1,0 +1,78 @@
+"""CPU checks of the C-ABI library: it builds, loads and exports every symbol
+``include/cui_born.h`` declares; argument validation answers without a GPU.
+No compute call is made here."""
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "cui_born.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(cui_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from comp_ui_toolbox_gb300 import build
+    build.build()
+    from comp_ui_toolbox_gb300.born import load_library
+    return load_library()
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for n in ["cui_born_plan_create", "cui_born_plan_destroy", "cui_born_forward", "cui_born_adjoint",
+              "cui_born_vjp", "cui_born_combined_host", "cui_born_size", "cui_last_error"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_python_mirror_binds_every_symbol():
+    from comp_ui_toolbox_gb300.born import _SIGNATURES
+    assert set(_SIGNATURES) == set(declared_functions())
+
+
+def test_status_strings_and_null_arguments(lib):
+    assert lib.cui_status_string(0) == b"CUI_OK"
+    assert lib.cui_status_string(2) == b"CUI_ERR_UNSUPPORTED_SETUP"
+    assert lib.cui_born_plan_destroy(None) == 0
+    n = C.c_int64()
+    assert lib.cui_born_size(None, C.byref(n), None) == 1
+    assert lib.cui_born_forward(None, None, 0, 1, None, 0, None) == 1
+    assert b"plan" in lib.cui_last_error()
+    out = C.c_void_p()
+    assert lib.cui_born_plan_create(None, 1, C.byref(out)) == 1
+    assert out.value is None
+
+
+def test_descriptor_validation_before_any_device_call(lib):
+    from comp_ui_toolbox_gb300.born import BornDesc
+    d = BornDesc()
+    d.n_dims = 4
+    out = C.c_void_p()
+    assert lib.cui_born_plan_create(C.byref(d), 1, C.byref(out)) == 1
+    assert b"n_dims" in lib.cui_last_error()
+    d.n_dims = 2
+    d.n_points_axis[0] = 8
+    d.n_points_axis[1] = 4
+    d.n_elements_axis[0] = 2
+    d.n_points_per_pitch[0] = 2
+    d.n_f_unique = 1
+    d.n_measurements = 0
+    assert lib.cui_born_plan_create(C.byref(d), 1, C.byref(out)) == 1
+    assert b"measurement" in lib.cui_last_error()
+
+
+def test_launch_counter_starts_readable(lib):
+    assert lib.cui_launch_count() >= 0

@@ -1,0 +1,232 @@
+"""GPU parity tests of the FP32 Born operator against the FP64 oracle.
+
+Every call goes through libcui_born.so's C-ABI (via the ctypes host mirror).
+Tolerance: relative L2 error <= 1e-5 against the FP64 oracle for every
+output (forward, adjoint, VJP), the bound the operator is specified to.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import adjoint_quick_cpu, forward_quick_cpu
+from oracle import configs
+from tests.helpers import make_operator, rel_l2
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5          # relative L2 vs FP64 oracle
+TOL_DOT = 1e-6      # dot-product (adjointness) test, relative to |Phi x| |y|
+
+CONFIGS = ["c0", "c1", "c2", "ragged", "c3"]
+_BUILT = {}
+
+
+def built(name):
+    if name not in _BUILT:
+        _BUILT[name] = configs.build(configs.small_config(name))
+    return _BUILT[name]
+
+
+def dev(x):
+    return torch.from_numpy(np.asarray(x, dtype=np.complex64)).cuda()
+
+
+def rand_obs(b, n_cols, seed):
+    rng = np.random.default_rng(seed)
+    n = b.op.n_observations
+    return rng.standard_normal((n, n_cols)) + 1j * rng.standard_normal((n, n_cols))
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_forward_adjoint_match_oracle(name):
+    b = built(name)
+    B = b.cfg.n_objects
+    op = make_operator(b, "lateral", max_objects=B)
+    gamma = configs.make_gamma(b.cfg)
+    u_ref = forward_quick_cpu(b.op, gamma)
+    u = op.forward(dev(gamma)).cpu().numpy()
+    assert u.shape == u_ref.shape
+    assert rel_l2(u, u_ref) <= TOL
+    y = rand_obs(b, B, 7)
+    g_ref = adjoint_quick_cpu(b.op, y)
+    g = op.adjoint(dev(y)).cpu().numpy()
+    assert rel_l2(g, g_ref) <= TOL
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "ragged", "c3"])
+def test_reference_form_matches_lateral_form(name):
+    """The reference's h_ref + indices_grid_FOV_shift give the same operator."""
+    b = built(name)
+    B = b.cfg.n_objects
+    op_ref = make_operator(b, "reference", max_objects=B)
+    op_lat = make_operator(b, "lateral", max_objects=B)
+    gamma = dev(configs.make_gamma(b.cfg, complex_values=True))
+    u_ref = op_ref.forward(gamma).cpu().numpy()
+    u_lat = op_lat.forward(gamma).cpu().numpy()
+    assert rel_l2(u_ref, u_lat) <= 1e-6
+    assert rel_l2(u_ref, forward_quick_cpu(b.op, gamma.cpu().numpy().astype(np.complex128))) <= TOL
+
+
+@pytest.mark.parametrize("name", ["c1", "ragged"])
+def test_host_path_matches_oracle(name):
+    """FP64 host buffers in, FP64 out: the MEX gateway's semantics."""
+    b = built(name)
+    B = b.cfg.n_objects
+    op = make_operator(b, "lateral", max_objects=B)
+    gamma = configs.make_gamma(b.cfg)
+    u = op.forward(gamma)
+    assert u.dtype == np.complex128
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
+    y = rand_obs(b, B, 3)
+    assert rel_l2(op.adjoint(y), adjoint_quick_cpu(b.op, y)) <= TOL
+    assert op.combined_scalar(0) == (b.op.n_observations, b.cfg.setup.n_points)
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_dot_product_adjointness(name):
+    b = built(name)
+    op = make_operator(b, "lateral", max_objects=1)
+    rng = np.random.default_rng(11)
+    P = b.cfg.setup.n_points
+    x = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    y = rand_obs(b, 1, 12)[:, 0]
+    Ax = op.forward(dev(x)).cpu().numpy().astype(np.complex128)
+    AHy = op.adjoint(dev(y)).cpu().numpy().astype(np.complex128)
+    lhs = np.vdot(y, Ax)
+    rhs = np.vdot(AHy, x)
+    assert abs(lhs - rhs) <= TOL_DOT * np.linalg.norm(Ax) * np.linalg.norm(y)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_vjp_matches_oracle(name):
+    b = built(name)
+    B = b.cfg.n_objects
+    op = make_operator(b, "lateral", max_objects=B)
+    gamma_true = configs.make_gamma(b.cfg)
+    u_meas = configs.add_noise(forward_quick_cpu(b.op, gamma_true), 30.0, seed=5)
+    rng = np.random.default_rng(21)
+    gamma = rng.standard_normal(gamma_true.shape)
+    r = forward_quick_cpu(b.op, gamma) - u_meas
+    grad_ref = adjoint_quick_cpu(b.op, r)
+    loss_ref = 0.5 * np.sum(np.abs(r) ** 2, axis=0)
+    grad, loss = op.vjp(dev(gamma), dev(u_meas))
+    assert rel_l2(grad.cpu().numpy(), grad_ref) <= TOL
+    np.testing.assert_allclose(loss.cpu().numpy(), loss_ref, rtol=TOL)
+    grad_h, loss_h = op.vjp(gamma, u_meas)
+    assert rel_l2(grad_h, grad_ref) <= TOL
+    np.testing.assert_allclose(loss_h, loss_ref, rtol=TOL)
+
+
+def test_vjp_central_finite_differences():
+    """d/dt 0.5||Phi(g + t d) - u||^2 at t=0 equals Re<grad, d> (step 1e-3 relative)."""
+    b = built("c1")
+    op = make_operator(b, "lateral", max_objects=1)
+    rng = np.random.default_rng(31)
+    P = b.cfg.setup.n_points
+    gamma = rng.standard_normal(P)
+    u_meas = configs.add_noise(forward_quick_cpu(b.op, configs.make_gamma(b.cfg))[:, 0], 30.0, seed=2)
+    grad, _ = op.vjp(gamma, u_meas)
+    d = rng.standard_normal(P)
+    h = 1e-3 * np.linalg.norm(gamma) / np.linalg.norm(d)
+    _, lp = op.vjp(gamma + h * d, u_meas)
+    _, lm = op.vjp(gamma - h * d, u_meas)
+    fd = (lp - lm) / (2 * h)
+    an = np.real(np.vdot(grad, d))
+    assert abs(fd - an) <= 2e-3 * abs(an)
+
+
+def test_torch_autograd_backward_is_adjoint():
+    from comp_ui_toolbox_gb300 import born_forward
+    b = built("c1")
+    op = make_operator(b, "lateral", max_objects=1)
+    rng = np.random.default_rng(41)
+    P = b.cfg.setup.n_points
+    g = dev(rng.standard_normal(P) + 1j * rng.standard_normal(P)).requires_grad_(True)
+    u_meas = dev(rand_obs(b, 1, 42)[:, 0])
+    u = born_forward(g, op)
+    loss = 0.5 * (u - u_meas).abs().pow(2).sum()
+    loss.backward()
+    grad_vjp, loss_vjp = op.vjp(g.detach(), u_meas)
+    assert rel_l2(g.grad.cpu().numpy(), grad_vjp.cpu().numpy()) <= 1e-6
+    assert abs(loss.item() - loss_vjp.item()) <= 1e-5 * loss.item()
+
+
+def test_deterministic_and_linear():
+    b = built("c2")
+    B = b.cfg.n_objects
+    op = make_operator(b, "lateral", max_objects=B)
+    g1 = dev(configs.make_gamma(b.cfg, seed=1))
+    g2 = dev(configs.make_gamma(b.cfg, seed=2))
+    u1 = op.forward(g1)
+    u1b = op.forward(g1)
+    assert torch.equal(u1, u1b)                      # bitwise reproducible
+    u2 = op.forward(g2)
+    u12 = op.forward(g1 + 2.0 * g2)
+    assert rel_l2(u12.cpu().numpy(), (u1 + 2.0 * u2).cpu().numpy()) <= 1e-6
+    z = op.forward(torch.zeros_like(g1))
+    assert torch.count_nonzero(z) == 0
+
+
+def test_leading_dimension_and_subset_of_columns():
+    """Column-major inputs with ld > rows and fewer columns than max_objects."""
+    import ctypes as C
+    b = built("c2")
+    op = make_operator(b, "lateral", max_objects=6)
+    P, N = b.cfg.setup.n_points, b.op.n_observations
+    gamma = configs.make_gamma(b.cfg)[:, :3]
+    ld = P + 5
+    buf = torch.zeros((3, ld), dtype=torch.complex64, device="cuda")
+    buf[:, :P] = dev(gamma.T)
+    ldu = N + 3
+    out = torch.full((3, ldu), 7.0 + 0j, dtype=torch.complex64, device="cuda")
+    st = op._lib.cui_born_forward(op._plan, buf.data_ptr(), ld, 3, out.data_ptr(), ldu,
+                                  torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    u = out[:, :N].cpu().numpy().T
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
+    assert torch.all(out[:, N:] == 7.0)              # padding rows untouched
+    del C
+
+
+def test_errors_are_reported():
+    from comp_ui_toolbox_gb300 import CuiError
+    b = built("c1")
+    op = make_operator(b, "lateral", max_objects=1)
+    with pytest.raises(CuiError) as ei:
+        op.forward(dev(np.zeros((b.cfg.setup.n_points, 2))))   # more columns than max_objects
+    assert ei.value.status == 1
+    # symmetric index map out of range (FOV narrower than the array): the reference would fail
+    b0 = built("c0")
+    with pytest.raises(CuiError) as ei:
+        make_operator(configs.BuiltOperator(b0.cfg, _with_map(b0), b0.table_rx, b0.table_tx, False), "reference")
+    assert ei.value.status == 2
+    # a map that is not the symmetric lateral shift is refused
+    b1 = built("c1")
+    bad = b1.op.shift.copy()
+    bad[0, 3] = bad[1, 3]
+    opb = _with_map(b1, bad)
+    with pytest.raises(CuiError) as ei:
+        make_operator(configs.BuiltOperator(b1.cfg, opb, b1.table_rx, b1.table_tx, True), "reference")
+    assert ei.value.status == 2
+
+
+def _with_map(b, shift=None):
+    import dataclasses
+    from oracle import shift_lateral, transfer_function
+    s = b.cfg.setup
+    if shift is None:
+        shift, _ = shift_lateral(s)
+    h_ref = b.op.h_ref if b.op.h_ref is not None else transfer_function(s, b.op.f_unique, 0, s.aa_rx_beta)
+    return dataclasses.replace(b.op, h_ref=h_ref, shift=shift)
+
+
+def test_native_kernels_launched():
+    from comp_ui_toolbox_gb300 import launch_count
+    b = built("c1")
+    op = make_operator(b, "lateral", max_objects=1)
+    n0 = launch_count()
+    op.forward(dev(configs.make_gamma(b.cfg)))
+    torch.cuda.synchronize()
+    assert launch_count() - n0 >= 3
