@@ -108,6 +108,7 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
 // shared-memory bytes the contraction kernels request
 size_t fwd_smem_bytes(const Plan* p, int nc);
 size_t adj_smem_bytes(const Plan* p, int nc);
+bool launch_shapes_ok(const Plan* p, std::string* why);
 
 }  // namespace cui
 

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <algorithm>
+#include <string>
 
 #include "cui_internal.cuh"
 
@@ -627,6 +628,17 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
 }
 
 }  // namespace
+
+bool launch_shapes_ok(const Plan* p, std::string* why) {
+    const int nc = pick_nc(p->max_slots_per_f);
+    const FwdShape f = fwd_shape(p, nc >= 16 ? 2 : 4);
+    const AdjShape a = adj_shape(p, nc >= 12 ? 2 : 4);
+    if (f.threads > 512 || a.threads > 512) {
+        *why = "launch shape exceeds 512 threads (too many points per pitch or elements for this build)";
+        return false;
+    }
+    return true;
+}
 
 size_t fwd_smem_bytes(const Plan* p, int nc) {
     return sizeof(float2) * (static_cast<size_t>(p->ppx) * p->Ni + static_cast<size_t>(p->Nx) * nc +

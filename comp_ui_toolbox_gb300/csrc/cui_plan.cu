@@ -296,6 +296,10 @@ cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
     if (fwd_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin) ||
         adj_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin))
         return set_error(CUI_ERR_UNSUPPORTED_SETUP, "grid line too long for the shared-memory staging of this build");
+    {
+        std::string why;
+        if (!launch_shapes_ok(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
+    }
 
     // ---- tables ----------------------------------------------------------------
     std::vector<float2> T;
