@@ -1,0 +1,293 @@
+"""Benchmark of the GB300 Born operator: forward + adjoint applies per second.
+
+Workload (default ``2d-gradient``): 2D, 512x512 FOV at 76.2 um, 128-element
+linear array, 11 quasi-plane waves (-20..20 deg), 192 frequencies over
+2-6 MHz, time-causal absorption.  One step = one gradient of
+0.5||Phi gamma - u||^2 (forward, residual, adjoint) at a seeded Gaussian
+gamma through the C-ABI (``cui_born_vjp``) -- one forward + adjoint apply.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Prints one JSON line.  ``value`` is applies/s over all ranks with inputs
+resident in HBM; ``e2e`` is the same metric through the host (FP64, MEX
+semantics) entry point, with host<->device copies inside the timed region.
+``--impl reference`` times the reference's CPU operator (its FP64
+restatement) on the host cores instead.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Born fwd+adj applies/s, % roofline; batched split-BF16 vs FP32 at rel err≤1e-5"
+ORACLE_NAME = {"2d-plain": "c0", "2d-gradient": "c1", "2d-batched": "c2", "3d": "c3"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="2d-gradient")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d.get("sm_max_mhz", 2070.0)), "measured"
+    return 6800.0, 2070.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(workload: str):
+    from oracle.cpu_baseline import time_sample
+    r = time_sample(ORACLE_NAME[workload], n_waves=1, n_freq=8)
+    return {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
+            "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
+
+
+def workload_config(w, B):
+    return {"workload": f"{w.name}: {'x'.join(map(str, w.n_points_axis))} FOV, {len(w.f)} frequencies, "
+                        f"{w.n_elements} elements, {len(w.waves)} waves, {w.absorption['kind']} medium; "
+                        f"one step = VJP of 0.5||Phi g - u||^2 (forward + adjoint)",
+            "n_points": w.n_points, "n_frequencies": len(w.f), "n_waves": len(w.waves),
+            "n_elements": w.n_elements, "n_objects": B,
+            "l2": "inputs larger than L2 (incident fields and transfer-function table, several GB, re-read every step)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from comp_ui_toolbox_gb300.workloads import workload
+    w = workload(args.workload)
+    B = 1
+    from oracle.cpu_baseline import time_sample
+    vals, secs = [], []
+    first = time_sample(ORACLE_NAME[args.workload], n_waves=1, n_freq=8, repeats=max(1, args.warmup + args.steps))
+    t_full = first["seconds_full_apply"]
+    value = first["applies_per_s"]
+    line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_full * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": workload_config(w, B),
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": first["cores"], "kind": "port",
+                             "sample": first["sample"]},
+            "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    del vals, secs
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from comp_ui_toolbox_gb300 import OperatorBorn, launch_count
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload(args.workload)
+    B = w.n_objects if args.workload == "2d-batched" else 1
+    t0 = time.perf_counter()
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=B)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    P, N = op.n_points, op.n_observations
+
+    # data: u = Phi gamma_true + 30 dB noise; the gradient is taken at a seeded Gaussian gamma
+    gamma_true = torch.from_numpy(w.gamma(n_objects=B).astype(np.complex64)).cuda()
+    u_clean = op.forward(gamma_true)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    noise = torch.randn(u_clean.shape, dtype=torch.complex64, device="cuda", generator=gen)
+    snr = 10 ** (-30 / 20)
+    u_meas = (u_clean + noise * (u_clean.abs().pow(2).mean().sqrt() / noise.abs().pow(2).mean().sqrt()) * snr).contiguous()
+    gamma = torch.randn((P, B), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
+
+    def step():
+        return op.vjp(gamma, u_meas)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    op.timing(True)
+    op.timing()  # clear
+    n0 = launch_count()
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            grad, loss = step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches = launch_count() - n0
+    kt = op.timing()
+    op.timing(False)
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * args.steps * B / (ms / 1e3)
+
+    # end to end through the host (FP64) entry point: copies inside the timed region
+    e2e_steps = args.e2e_steps or max(1, min(args.steps, 5))
+    g_host = gamma.cpu().numpy().astype(np.complex128)
+    u_host = u_meas.cpu().numpy().astype(np.complex128)
+    op.vjp(g_host, u_host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        grad_h, loss_h = op.vjp(g_host, u_host)
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": e2e_steps * B / t_e2e, "unit": "applies/s",
+           "h2d_bytes_per_step": 8 * (P + N) * B, "d2h_bytes_per_step": 8 * P * B + 4 * B,
+           "path": "cui_born_vjp_host: FP64 host buffers -> FP32 pinned staging -> H2D -> VJP -> D2H -> FP64"}
+
+    # roofline of the dominant contraction kernel
+    hbm, sm_max, peak_kind = peaks()
+    info = op.info
+    macs = info["contraction_macs"] * B  # complex MACs of one dense apply
+    dom = "forward" if kt["ms_forward"] >= kt["ms_adjoint"] else "adjoint"
+    n_l = kt["n_" + dom] or 1
+    t_launch = kt["ms_" + dom] / n_l / 1e3
+    phi_bytes = 8.0 * macs                                    # Phi-equivalent bytes (reference formulation)
+    compulsory = info["table_bytes"] + info["incident_bytes"] + 8 * B * (P if dom == "forward" else P)
+    flops = 8.0 * macs
+    sm_mhz = None
+    clk = clocks.summary()
+    sm_mhz = clk.get("sm_mhz") or sm_max
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12             # TFLOP/s of the CUDA cores at the sampled clock
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        tj = json.loads(tf.read_text())
+        traffic = tj.get(f"{args.workload}:{dom}")
+    roofline = {"bound": "hbm", "achieved": phi_bytes / t_launch / 1e9, "peak": hbm, "unit": "GB/s",
+                "frac": phi_bytes / t_launch / 1e9 / hbm, "traffic": traffic,
+                "kernel": f"{dom} contraction ({'fwd_dense_kernel' if dom == 'forward' else 'adj_dense_kernel'})",
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "achieved_definition": "Phi-equivalent bytes (8 B per complex MAC, the reference's materialised "
+                                       "Phi read once) / average launch time",
+                "compulsory_bytes": compulsory, "compulsory_frac": compulsory / t_launch / 1e9 / hbm,
+                "fp32": {"achieved_tflops": flops / t_launch / 1e12, "peak_tflops": fp32_peak,
+                         "frac": flops / t_launch / 1e12 / fp32_peak,
+                         "peak_definition": "152 SMs x 128 FP32 lanes x 2 flops x median sampled SM clock"},
+                "launch_ms": {"forward": kt["ms_forward"] / max(1, kt["n_forward"]),
+                              "adjoint": kt["ms_adjoint"] / max(1, kt["n_adjoint"])}}
+
+    line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": workload_config(w, B),
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "clocks": clk,
+            "plan": {"build_s": t_build, "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
+                     "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs},
+            "loss": float(loss.sum().item())}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.workload)
+        except Exception as exc:  # report, never hide
+            line["cpu_baseline"] = {"value": None, "error": repr(exc)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    op.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

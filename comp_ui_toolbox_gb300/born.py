@@ -70,6 +70,30 @@ class BornDesc(C.Structure):
                 ("measurements", C.POINTER(MeasurementDesc)), ("device", C.c_int32)]
 
 
+class AbsorptionDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("c", C.c_double), ("constant_db", C.c_double), ("slope_db", C.c_double),
+                ("exponent", C.c_double), ("f_ref", C.c_double), ("dispersion", C.c_int32)]
+
+
+class WaveDesc(C.Structure):
+    _fields_ = [("n_f", C.c_int32), ("indices_f_to_unique", C.POINTER(C.c_int32)), ("v_d", C.c_void_p),
+                ("n_mixes", C.c_int32), ("mixes", C.POINTER(MixDesc))]
+
+
+class SetupDesc(C.Structure):
+    _fields_ = [("n_dims", C.c_int32), ("n_points_axis", C.c_int32 * 3), ("delta_axis", C.c_double * 3),
+                ("z_start", C.c_double), ("n_elements_axis", C.c_int32 * 2), ("pitch_axis", C.c_double * 2),
+                ("width_axis", C.c_double * 2), ("n_face_axis", C.c_int32 * 2), ("absorption", AbsorptionDesc),
+                ("aa_tx_beta", C.c_double), ("aa_rx_beta", C.c_double), ("n_f_unique", C.c_int32),
+                ("f_unique", C.POINTER(C.c_double)), ("n_measurements", C.c_int32),
+                ("waves", C.POINTER(WaveDesc)), ("device", C.c_int32)]
+
+
+class BornTiming(C.Structure):
+    _fields_ = [("n_forward", C.c_int64), ("n_adjoint", C.c_int64), ("ms_forward", C.c_double),
+                ("ms_adjoint", C.c_double)]
+
+
 class BornInfo(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("n_points", "n_observations", "n_elements", "n_slots", "n_f_unique",
                                          "table_bytes", "incident_bytes", "workspace_bytes", "contraction_macs")]
@@ -80,6 +104,7 @@ _lib = None
 # every symbol include/cui_born.h declares, with its ctypes signature
 _SIGNATURES = {
     "cui_born_plan_create": (C.c_int, [C.POINTER(BornDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    "cui_born_plan_create_setup": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.POINTER(C.c_void_p)]),
     "cui_born_plan_destroy": (C.c_int, [C.c_void_p]),
     "cui_born_plan_info": (C.c_int, [C.c_void_p, C.POINTER(BornInfo)]),
     "cui_born_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -91,6 +116,8 @@ _SIGNATURES = {
                                          C.c_int64]),
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
+    "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
+    "cui_born_timing_read": (C.c_int, [C.c_void_p, C.POINTER(BornTiming)]),
     "cui_status_string": (C.c_char_p, [C.c_int]),
     "cui_last_error": (C.c_char_p, []),
     "cui_launch_count": (C.c_int64, []),
@@ -134,6 +161,27 @@ def _i32(a) -> np.ndarray:
 def _c128_f(a) -> np.ndarray:
     """Complex FP64 array in column-major (MATLAB) order."""
     return np.asfortranarray(np.asarray(a, dtype=np.complex128))
+
+
+def _get(obj, key):
+    return obj[key] if isinstance(obj, dict) else getattr(obj, key)
+
+
+def _mix_array(mixes_in, weight_key, keep):
+    """ctypes array of cui_mix_desc; ``weight_key`` names the prefactor / response field."""
+    mixes = (MixDesc * max(1, len(mixes_in)))()
+    keep.append(mixes)
+    for k, mx in enumerate(mixes_in):
+        mf = _i32(np.asarray(_get(mx, "f_idx")) + 1)
+        act = _i32(np.asarray(_get(mx, "active")) + 1)
+        wts = _c128_f(_get(mx, weight_key))
+        keep += [mf, act, wts]
+        mixes[k].n_f = len(mf)
+        mixes[k].indices_f_to_unique = mf.ctypes.data_as(C.POINTER(C.c_int32))
+        mixes[k].n_active = len(act)
+        mixes[k].indices_active = act.ctypes.data_as(C.POINTER(C.c_int32))
+        mixes[k].prefactors = wts.ctypes.data
+    return mixes
 
 
 class OperatorBorn:
@@ -188,32 +236,87 @@ class OperatorBorn:
             d.indices_grid_FOV_shift = m.ctypes.data_as(C.POINTER(C.c_int32))
         meas = (MeasurementDesc * len(measurements))()
         for w, ms in enumerate(measurements):
-            get = (lambda o, k: o[k]) if isinstance(ms, dict) else getattr
-            f_idx = _i32(np.asarray(get(ms, "f_idx")) + 1)
-            p_in = _c128_f(get(ms, "p_incident"))
-            mixes_in = list(get(ms, "mixes"))
-            mixes = (MixDesc * max(1, len(mixes_in)))()
-            keep += [f_idx, p_in, mixes]
-            for k, mx in enumerate(mixes_in):
-                gm = (lambda o, key: o[key]) if isinstance(mx, dict) else getattr
-                mf = _i32(np.asarray(gm(mx, "f_idx")) + 1)
-                act = _i32(np.asarray(gm(mx, "active")) + 1)
-                pref = _c128_f(gm(mx, "pref"))
-                keep += [mf, act, pref]
-                mixes[k].n_f = len(mf)
-                mixes[k].indices_f_to_unique = mf.ctypes.data_as(C.POINTER(C.c_int32))
-                mixes[k].n_active = len(act)
-                mixes[k].indices_active = act.ctypes.data_as(C.POINTER(C.c_int32))
-                mixes[k].prefactors = pref.ctypes.data
+            f_idx = _i32(np.asarray(_get(ms, "f_idx")) + 1)
+            p_in = _c128_f(_get(ms, "p_incident"))
+            mixes_in = list(_get(ms, "mixes"))
+            keep += [f_idx, p_in]
             meas[w].n_f = len(f_idx)
             meas[w].indices_f_to_unique = f_idx.ctypes.data_as(C.POINTER(C.c_int32))
             meas[w].p_incident = p_in.ctypes.data
             meas[w].n_mixes = len(mixes_in)
-            meas[w].mixes = mixes
+            meas[w].mixes = _mix_array(mixes_in, "pref", keep)
         d.n_measurements = len(measurements)
         d.measurements = meas
         d.device = int(device)
         _check(lib.cui_born_plan_create(C.byref(d), int(max_objects), C.byref(self._plan)))
+        self._finish(max_objects, device)
+
+    @classmethod
+    def from_setup(cls, *, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_start: float,
+                   n_elements_axis: Sequence[int], pitch_axis: Sequence[float], width_axis: Sequence[float],
+                   n_face_axis: Sequence[int], absorption: dict, f_unique, waves,
+                   aa_tx_beta: Optional[float] = 0.5, aa_rx_beta: Optional[float] = 0.5,
+                   device: int = 0, max_objects: int = 1) -> "OperatorBorn":
+        """Plan whose tables the GPU computes from the discretised setup.
+
+        ``absorption``: ``{"kind": "none"|"time_causal", "c", "constant_db", "slope_db", "exponent",
+        "f_ref", "dispersion"}``.  ``waves``: objects or dicts with ``f_idx`` (0-based global
+        frequency indices), ``v_d`` ``(F_w, E)`` normal velocities and ``mixes`` (``f_idx``,
+        ``active``, ``response`` ``(F_mix, n_active)`` receive responses).  ``aa_*_beta=None``
+        switches an anti-aliasing filter off.
+        """
+        self = cls.__new__(cls)
+        lib = load_library()
+        self._lib = lib
+        self._plan = C.c_void_p()
+        keep = []
+        d = SetupDesc()
+        nd = len(n_points_axis)
+        d.n_dims = nd
+        for k in range(nd):
+            d.n_points_axis[k] = int(n_points_axis[k])
+            d.delta_axis[k] = float(delta_axis[k])
+        for k in range(nd - 1):
+            d.n_elements_axis[k] = int(n_elements_axis[k])
+            d.pitch_axis[k] = float(pitch_axis[k])
+            d.width_axis[k] = float(width_axis[k])
+            d.n_face_axis[k] = int(n_face_axis[k])
+        d.z_start = float(z_start)
+        a = AbsorptionDesc()
+        a.kind = {"none": 0, "time_causal": 1}[absorption.get("kind", "none")]
+        a.c = float(absorption.get("c", 1500.0))
+        a.constant_db = float(absorption.get("constant_db", 0.0))
+        a.slope_db = float(absorption.get("slope_db", 0.0))
+        a.exponent = float(absorption.get("exponent", 1.0))
+        a.f_ref = float(absorption.get("f_ref", 4e6))
+        a.dispersion = int(bool(absorption.get("dispersion", True)))
+        d.absorption = a
+        d.aa_tx_beta = -1.0 if aa_tx_beta is None else float(aa_tx_beta)
+        d.aa_rx_beta = -1.0 if aa_rx_beta is None else float(aa_rx_beta)
+        f = np.ascontiguousarray(np.asarray(f_unique, dtype=np.float64))
+        keep.append(f)
+        d.n_f_unique = len(f)
+        d.f_unique = f.ctypes.data_as(C.POINTER(C.c_double))
+        wv = (WaveDesc * len(waves))()
+        for w, wave in enumerate(waves):
+            f_idx = _i32(np.asarray(_get(wave, "f_idx")) + 1)
+            v_d = _c128_f(_get(wave, "v_d"))
+            mixes_in = list(_get(wave, "mixes"))
+            keep += [f_idx, v_d]
+            wv[w].n_f = len(f_idx)
+            wv[w].indices_f_to_unique = f_idx.ctypes.data_as(C.POINTER(C.c_int32))
+            wv[w].v_d = v_d.ctypes.data
+            wv[w].n_mixes = len(mixes_in)
+            wv[w].mixes = _mix_array(mixes_in, "response", keep)
+        d.n_measurements = len(waves)
+        d.waves = wv
+        d.device = int(device)
+        _check(lib.cui_born_plan_create_setup(C.byref(d), int(max_objects), C.byref(self._plan)))
+        self._finish(max_objects, device)
+        return self
+
+    def _finish(self, max_objects, device):
+        lib = self._lib
         self.max_objects = int(max_objects)
         info = BornInfo()
         _check(lib.cui_born_plan_info(self._plan, C.byref(info)))
@@ -239,6 +342,15 @@ class OperatorBorn:
 
     def __exit__(self, *exc):
         self.close()
+
+    def timing(self, enable: Optional[bool] = None) -> dict:
+        """Enable/disable per-kernel event timing, or read (and clear) the sums."""
+        if enable is not None:
+            _check(self._lib.cui_born_timing_enable(self._plan, int(bool(enable))))
+            return {}
+        t = BornTiming()
+        _check(self._lib.cui_born_timing_read(self._plan, C.byref(t)))
+        return {n: getattr(t, n) for n, _ in BornTiming._fields_}
 
     @property
     def size(self):

@@ -27,6 +27,21 @@ namespace cui {
 // (incident waves sharing one frequency) one thread block processes per pass.
 constexpr int kMaxNC = 16;
 
+// Observation-row and mixing metadata built on the host before upload.
+struct HostMeta {
+    std::vector<int> row_slot, row_mix, row_fl, mix_nact, mix_nf, mix_act_off, act, pos, slot_row_ptr, slot_rows;
+    std::vector<int64_t> mix_pref_off;
+    std::vector<float2> pref;
+};
+
+// One measurement as seen by the metadata builder (both descriptor forms).
+struct MeasIn {
+    int n_f;
+    const int32_t* f_idx;         // 1-based global frequency indices
+    int n_mixes;
+    const cui_mix_desc* mixes;
+};
+
 struct Plan {
     int device = 0;
     int n_dims = 2;
@@ -89,6 +104,16 @@ struct Plan {
     float2* d_stage_aux = nullptr;
     float* d_stage_loss = nullptr;
 
+    // host copies kept after creation (launch planning, table builders)
+    std::vector<int> h_f_slot_ptr, h_f_slot_list, h_slot_f;
+    HostMeta h_meta;                 // emptied once uploaded
+
+    // per-kernel timing (diagnostics): event pairs around contraction launches
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_kind;        // 0 forward, 1 adjoint; pair i uses ev_pool[2i], ev_pool[2i+1]
+    size_t ev_used = 0;
+
     std::vector<void*> allocations;  // every device allocation (freed on destroy)
 };
 
@@ -96,6 +121,16 @@ struct Plan {
 cui_status set_error(cui_status s, const std::string& msg);
 cui_status check_cuda(cudaError_t e, const char* what);
 void count_launch(int n = 1);
+
+// plan construction stages shared by both descriptor forms -----------------
+cui_status init_geometry(Plan& p, int n_dims, const int32_t* npts, const int32_t* nel, const int32_t* ppp, int F,
+                         int W, int max_objects);
+// pref_scale (optional, per global frequency) multiplies every prefactor
+cui_status build_metadata(Plan& p, const std::vector<MeasIn>& ms, const std::vector<double2>* pref_scale,
+                          std::vector<int>& meas_slot0);
+cui_status select_device_and_shapes(Plan& p, int device);
+cui_status upload_metadata_and_workspace(Plan& p);
+cui_status device_alloc(Plan& p, void** ptr, size_t bytes);
 
 // apply entry points used by the host wrappers ----------------------------
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu,
@@ -109,6 +144,10 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
 size_t fwd_smem_bytes(const Plan* p, int nc);
 size_t adj_smem_bytes(const Plan* p, int nc);
 bool launch_shapes_ok(const Plan* p, std::string* why);
+// timing hooks around a contraction launch (no-ops unless timing is enabled)
+cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st);
+cudaError_t timing_end(Plan* p, cudaStream_t st);
+void timing_release(Plan* p);
 
 }  // namespace cui
 

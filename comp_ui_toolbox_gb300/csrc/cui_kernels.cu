@@ -545,9 +545,11 @@ cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, c
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(p->fwd_groups * p->Ey, p->F, B * a.npass);
+    if ((e = timing_begin(const_cast<Plan*>(p), 0, st)) != cudaSuccess) return e;
     fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
     count_launch();
-    return cudaGetLastError();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return timing_end(const_cast<Plan*>(p), st);
 }
 
 template <int NC>
@@ -566,9 +568,11 @@ cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(p->Ny * p->Nz, p->adj_nfc, B);
+    if ((e = timing_begin(const_cast<Plan*>(p), 1, st)) != cudaSuccess) return e;
     adj_dense_kernel<NC, KJ><<<grid, sh.threads, smem, st>>>(a);
     count_launch();
-    return cudaGetLastError();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return timing_end(const_cast<Plan*>(p), st);
 }
 
 int grid_1d(int64_t n, int threads) {
@@ -638,6 +642,33 @@ bool launch_shapes_ok(const Plan* p, std::string* why) {
         return false;
     }
     return true;
+}
+
+cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st) {
+    if (!p->timing) return cudaSuccess;
+    while (p->ev_pool.size() < 2 * (p->ev_used + 1)) {
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) return e;
+        p->ev_pool.push_back(ev);
+    }
+    if (p->ev_kind.size() < p->ev_used + 1) p->ev_kind.resize(p->ev_used + 1);
+    p->ev_kind[p->ev_used] = kind;
+    return cudaEventRecord(p->ev_pool[2 * p->ev_used], st);
+}
+
+cudaError_t timing_end(Plan* p, cudaStream_t st) {
+    if (!p->timing) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(p->ev_pool[2 * p->ev_used + 1], st);
+    ++p->ev_used;
+    return e;
+}
+
+void timing_release(Plan* p) {
+    for (cudaEvent_t ev : p->ev_pool) cudaEventDestroy(ev);
+    p->ev_pool.clear();
+    p->ev_kind.clear();
+    p->ev_used = 0;
 }
 
 size_t fwd_smem_bytes(const Plan* p, int nc) {

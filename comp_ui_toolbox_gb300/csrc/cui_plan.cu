@@ -62,6 +62,7 @@ cudaError_t upload(Plan& p, T** ptr, const std::vector<T>& h) {
 }
 
 void free_plan(Plan& p) {
+    timing_release(&p);
     for (void* v : p.allocations) cudaFree(v);
     p.allocations.clear();
     if (p.h_stage_in) cudaFreeHost(p.h_stage_in);
@@ -164,48 +165,54 @@ cui_status build_table(Plan& p, const cui_born_desc* d, std::vector<float2>& T) 
     return CUI_OK;
 }
 
-cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
-    if (!d) return set_error(CUI_ERR_INVALID_ARG, "desc is NULL");
-    if (d->n_dims != 2 && d->n_dims != 3) return set_error(CUI_ERR_INVALID_ARG, "n_dims must be 2 or 3");
-    if (max_objects < 1) return set_error(CUI_ERR_INVALID_ARG, "max_objects must be >= 1");
-    const int nl = d->n_dims - 1;
-    for (int k = 0; k < d->n_dims; ++k)
-        if (d->n_points_axis[k] < 1) return set_error(CUI_ERR_INVALID_ARG, "n_points_axis must be positive");
-    for (int k = 0; k < nl; ++k)
-        if (d->n_elements_axis[k] < 1 || d->n_points_per_pitch[k] < 1)
-            return set_error(CUI_ERR_INVALID_ARG, "n_elements_axis / n_points_per_pitch must be positive");
-    if (d->n_f_unique < 1) return set_error(CUI_ERR_INVALID_ARG, "n_f_unique must be positive");
-    if (d->n_measurements < 1 || !d->measurements) return set_error(CUI_ERR_INVALID_ARG, "no measurements");
+}  // namespace
 
-    p.n_dims = d->n_dims;
-    p.Nx = d->n_points_axis[0];
-    p.Ny = (d->n_dims == 3) ? d->n_points_axis[1] : 1;
-    p.Nz = d->n_points_axis[d->n_dims - 1];
-    p.Ex = d->n_elements_axis[0];
-    p.Ey = (d->n_dims == 3) ? d->n_elements_axis[1] : 1;
-    p.ppx = d->n_points_per_pitch[0];
-    p.ppy = (d->n_dims == 3) ? d->n_points_per_pitch[1] : 1;
+cui_status init_geometry(Plan& p, int n_dims, const int32_t* npts, const int32_t* nel, const int32_t* ppp, int F,
+                         int W, int max_objects) {
+    if (n_dims != 2 && n_dims != 3) return set_error(CUI_ERR_INVALID_ARG, "n_dims must be 2 or 3");
+    if (max_objects < 1) return set_error(CUI_ERR_INVALID_ARG, "max_objects must be >= 1");
+    for (int k = 0; k < n_dims; ++k)
+        if (npts[k] < 1) return set_error(CUI_ERR_INVALID_ARG, "n_points_axis must be positive");
+    for (int k = 0; k < n_dims - 1; ++k)
+        if (nel[k] < 1 || ppp[k] < 1)
+            return set_error(CUI_ERR_INVALID_ARG, "n_elements_axis / n_points_per_pitch must be positive");
+    if (F < 1) return set_error(CUI_ERR_INVALID_ARG, "n_f_unique must be positive");
+    if (W < 1) return set_error(CUI_ERR_INVALID_ARG, "no measurements");
+    p.n_dims = n_dims;
+    p.Nx = npts[0];
+    p.Ny = (n_dims == 3) ? npts[1] : 1;
+    p.Nz = npts[n_dims - 1];
+    p.Ex = nel[0];
+    p.Ey = (n_dims == 3) ? nel[1] : 1;
+    p.ppx = ppp[0];
+    p.ppy = (n_dims == 3) ? ppp[1] : 1;
     p.Nox = p.Nx + (p.Ex - 1) * p.ppx;
-    p.Noy = (d->n_dims == 3) ? p.Ny + (p.Ey - 1) * p.ppy : 1;
+    p.Noy = (n_dims == 3) ? p.Ny + (p.Ey - 1) * p.ppy : 1;
     p.P = static_cast<int64_t>(p.Nx) * p.Ny * p.Nz;
     p.E = p.Ex * p.Ey;
-    p.F = d->n_f_unique;
-    p.W = d->n_measurements;
+    p.F = F;
+    p.W = W;
     p.max_objects = max_objects;
     p.Nj_max = (p.Nx + p.ppx - 1) / p.ppx;
     p.Ni = 8 + p.Nj_max + p.Ex + 8;
     if (p.ppx > 16) return set_error(CUI_ERR_UNSUPPORTED_SETUP, "more than 16 grid points per pitch");
+    if (p.P > (int64_t(1) << 31) - 1) return set_error(CUI_ERR_UNSUPPORTED_SETUP, "more than 2^31-1 grid points");
+    return CUI_OK;
+}
 
-    // ---- slots, observation rows, mixes ------------------------------------
+#define CUI_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return check_cuda(e_, #x); } while (0)
+
+cui_status build_metadata(Plan& p, const std::vector<MeasIn>& ms, const std::vector<double2>* pref_scale,
+                          std::vector<int>& meas_slot0) {
     std::vector<int> slot_f;
-    std::vector<int> meas_slot0(p.W);
+    meas_slot0.assign(p.W, 0);
     for (int w = 0; w < p.W; ++w) {
-        const cui_measurement_desc& m = d->measurements[w];
-        if (m.n_f < 1 || !m.indices_f_to_unique || !m.p_incident || m.n_mixes < 0 || (m.n_mixes > 0 && !m.mixes))
+        const MeasIn& m = ms[w];
+        if (m.n_f < 1 || !m.f_idx || m.n_mixes < 0 || (m.n_mixes > 0 && !m.mixes))
             return set_error(CUI_ERR_INVALID_ARG, "invalid measurement " + std::to_string(w));
         meas_slot0[w] = static_cast<int>(slot_f.size());
         for (int k = 0; k < m.n_f; ++k) {
-            const int fg = m.indices_f_to_unique[k] - 1;
+            const int fg = m.f_idx[k] - 1;
             if (fg < 0 || fg >= p.F) return set_error(CUI_ERR_INVALID_ARG, "indices_f_to_unique out of range");
             slot_f.push_back(fg);
         }
@@ -226,7 +233,7 @@ cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
     std::vector<float2> pref;
     int mix_id = 0;
     for (int w = 0; w < p.W; ++w) {
-        const cui_measurement_desc& m = d->measurements[w];
+        const MeasIn& m = ms[w];
         for (int k = 0; k < m.n_mixes; ++k, ++mix_id) {
             const cui_mix_desc& x = m.mixes[k];
             if (x.n_f < 0 || x.n_active < 0 || (x.n_f > 0 && !x.indices_f_to_unique) ||
@@ -245,14 +252,28 @@ cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
                 act.push_back(e);
             }
             pos.insert(pos.end(), mpos.begin(), mpos.end());
-            for (int64_t i = 0; i < static_cast<int64_t>(x.n_f) * x.n_active; ++i) pref.push_back(to_f2(x.prefactors[i]));
+            std::vector<int> fm_of(x.n_f);
             for (int fl = 0; fl < x.n_f; ++fl) {
                 const int fm = x.indices_f_to_unique[fl] - 1;
                 if (fm < 0 || fm >= m.n_f) return set_error(CUI_ERR_INVALID_ARG, "mix indices_f_to_unique out of range");
+                fm_of[fl] = fm;
                 row_slot.push_back(meas_slot0[w] + fm);
                 row_mix.push_back(mix_id);
                 row_fl.push_back(fl);
             }
+            for (int a = 0; a < x.n_active; ++a)
+                for (int fl = 0; fl < x.n_f; ++fl) {
+                    const cui_complex64 c = x.prefactors[static_cast<int64_t>(a) * x.n_f + fl];
+                    if (!std::isfinite(c.re) || !std::isfinite(c.im))
+                        return set_error(CUI_ERR_NUMERIC, "non-finite prefactor");
+                    if (pref_scale) {
+                        const double2 sc = (*pref_scale)[m.f_idx[fm_of[fl]] - 1];
+                        pref.push_back(make_float2(static_cast<float>(sc.x * c.re - sc.y * c.im),
+                                                   static_cast<float>(sc.x * c.im + sc.y * c.re)));
+                    } else {
+                        pref.push_back(to_f2(c));
+                    }
+                }
         }
     }
     p.n_mix = mix_id;
@@ -265,46 +286,123 @@ cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
         std::vector<int> fill(slot_row_ptr.begin(), slot_row_ptr.end() - 1);
         for (int64_t r = 0; r < p.n_obs; ++r) slot_rows[fill[row_slot[r]]++] = static_cast<int>(r);
     }
+    p.h_f_slot_ptr = f_slot_ptr;
+    p.h_f_slot_list = f_slot_list;
+    p.h_slot_f = slot_f;
+    // device uploads happen in upload_metadata once the device is selected
+    p.h_meta.row_slot.swap(row_slot);
+    p.h_meta.row_mix.swap(row_mix);
+    p.h_meta.row_fl.swap(row_fl);
+    p.h_meta.mix_nact.swap(mix_nact);
+    p.h_meta.mix_nf.swap(mix_nf);
+    p.h_meta.mix_act_off.swap(mix_act_off);
+    p.h_meta.act.swap(act);
+    p.h_meta.pos.swap(pos);
+    p.h_meta.mix_pref_off.swap(mix_pref_off);
+    p.h_meta.pref.swap(pref);
+    p.h_meta.slot_row_ptr.swap(slot_row_ptr);
+    p.h_meta.slot_rows.swap(slot_rows);
+    return CUI_OK;
+}
 
-    // ---- launch geometry and scratch sizes -----------------------------------
+cui_status select_device_and_shapes(Plan& p, int device) {
     const int n_lines = p.Ny * p.Nz;
-    const int64_t gsz = static_cast<int64_t>(p.S) * max_objects * p.E * sizeof(float2);
+    const int64_t gsz = static_cast<int64_t>(p.S) * p.max_objects * p.E * sizeof(float2);
     int groups = std::max(1, std::min(n_lines, (2048 + p.F * p.Ey - 1) / (p.F * p.Ey)));
-    groups = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(groups, std::max<int64_t>(1, static_cast<int64_t>(kPartBudget) / std::max<int64_t>(gsz, 1)))));
+    groups = static_cast<int>(std::max<int64_t>(
+        1, std::min<int64_t>(groups, std::max<int64_t>(1, static_cast<int64_t>(kPartBudget) / std::max<int64_t>(gsz, 1)))));
     p.fwd_lines_per_group = (n_lines + groups - 1) / groups;
     p.fwd_groups = (n_lines + p.fwd_lines_per_group - 1) / p.fwd_lines_per_group;
-    const int64_t gpart = static_cast<int64_t>(max_objects) * p.P * sizeof(float2);
+    const int64_t gpart = static_cast<int64_t>(p.max_objects) * p.P * sizeof(float2);
     int nfc = std::max(1, std::min(p.F, (4096 + n_lines - 1) / n_lines));
-    nfc = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(nfc, std::max<int64_t>(1, static_cast<int64_t>(kPartBudget) / std::max<int64_t>(gpart, 1)))));
+    nfc = static_cast<int>(std::max<int64_t>(
+        1, std::min<int64_t>(nfc, std::max<int64_t>(1, static_cast<int64_t>(kPartBudget) / std::max<int64_t>(gpart, 1)))));
     p.adj_fchunk = (p.F + nfc - 1) / nfc;
     p.adj_nfc = (p.F + p.adj_fchunk - 1) / p.adj_fchunk;
 
-    // ---- device ----------------------------------------------------------------
     int n_dev = 0;
     if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
         return set_error(CUI_ERR_NO_DEVICE, "no CUDA device (combined_quick_gpu:NoCUDADevices)");
-    if (d->device < 0 || d->device >= n_dev)
+    if (device < 0 || device >= n_dev)
         return set_error(CUI_ERR_NO_DEVICE, "invalid device index (combined_quick_gpu:InvalidCUDADevice)");
-    p.device = d->device;
-    cudaError_t ce = cudaSetDevice(p.device);
-    if (ce != cudaSuccess) return check_cuda(ce, "cudaSetDevice");
+    p.device = device;
+    CUI_TRY(cudaSetDevice(p.device));
     int smem_optin = 0;
-    ce = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device);
-    if (ce != cudaSuccess) return check_cuda(ce, "cudaDeviceGetAttribute");
+    CUI_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device));
     int nc = 1;
     while (nc < p.max_slots_per_f && nc < kMaxNC) nc = (nc < 8) ? nc * 2 : nc + 4;
     if (fwd_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin) ||
         adj_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin))
         return set_error(CUI_ERR_UNSUPPORTED_SETUP, "grid line too long for the shared-memory staging of this build");
-    {
-        std::string why;
-        if (!launch_shapes_ok(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
-    }
+    std::string why;
+    if (!launch_shapes_ok(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
+    return CUI_OK;
+}
 
-    // ---- tables ----------------------------------------------------------------
-    std::vector<float2> T;
-    cui_status st = build_table(p, d, T);
+cui_status upload_metadata_and_workspace(Plan& p) {
+    HostMeta& h = p.h_meta;
+    CUI_TRY(upload(p, &p.f_slot_ptr, p.h_f_slot_ptr));
+    CUI_TRY(upload(p, &p.f_slot_list, p.h_f_slot_list));
+    CUI_TRY(upload(p, &p.row_slot, h.row_slot));
+    CUI_TRY(upload(p, &p.row_mix, h.row_mix));
+    CUI_TRY(upload(p, &p.row_fl, h.row_fl));
+    CUI_TRY(upload(p, &p.mix_nact, h.mix_nact));
+    CUI_TRY(upload(p, &p.mix_nf, h.mix_nf));
+    CUI_TRY(upload(p, &p.mix_pref_off, h.mix_pref_off));
+    CUI_TRY(upload(p, &p.mix_act_off, h.mix_act_off));
+    CUI_TRY(upload(p, &p.act, h.act));
+    CUI_TRY(upload(p, &p.pref, h.pref));
+    CUI_TRY(upload(p, &p.pos, h.pos));
+    CUI_TRY(upload(p, &p.slot_row_ptr, h.slot_row_ptr));
+    CUI_TRY(upload(p, &p.slot_rows, h.slot_rows));
+    p.h_meta = HostMeta();
+
+    const int B = p.max_objects;
+    const size_t part_fwd = static_cast<size_t>(p.fwd_groups) * p.S * B * p.E;
+    const size_t part_adj = static_cast<size_t>(p.adj_nfc) * B * p.P;
+    p.ws_part_bytes = std::max(part_fwd, part_adj) * sizeof(float2);
+    CUI_TRY(dalloc(p, &p.ws_part, std::max(part_fwd, part_adj)));
+    CUI_TRY(dalloc(p, &p.ws_G, static_cast<size_t>(p.S) * B * p.E));
+    CUI_TRY(dalloc(p, &p.ws_r, static_cast<size_t>(p.n_obs) * B));
+    CUI_TRY(dalloc(p, &p.ws_loss, loss_workspace_floats(B)));
+    p.workspace_bytes = p.ws_part_bytes +
+                        sizeof(float2) * (static_cast<size_t>(p.S) * B * p.E + static_cast<size_t>(p.n_obs) * B) +
+                        sizeof(float) * loss_workspace_floats(B);
+    return CUI_OK;
+}
+
+cui_status device_alloc(Plan& p, void** ptr, size_t bytes) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) return check_cuda(e, "cudaMalloc");
+    p.allocations.push_back(v);
+    *ptr = v;
+    return CUI_OK;
+}
+
+namespace {
+
+cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
+    if (!d) return set_error(CUI_ERR_INVALID_ARG, "desc is NULL");
+    cui_status st = init_geometry(p, d->n_dims, d->n_points_axis, d->n_elements_axis, d->n_points_per_pitch,
+                                  d->n_f_unique, d->n_measurements, max_objects);
     if (st != CUI_OK) return st;
+    if (!d->measurements) return set_error(CUI_ERR_INVALID_ARG, "no measurements");
+    std::vector<MeasIn> ms(p.W);
+    for (int w = 0; w < p.W; ++w) {
+        const cui_measurement_desc& m = d->measurements[w];
+        if (!m.p_incident) return set_error(CUI_ERR_INVALID_ARG, "invalid measurement " + std::to_string(w));
+        ms[w] = MeasIn{m.n_f, m.indices_f_to_unique, m.n_mixes, m.mixes};
+    }
+    std::vector<int> meas_slot0;
+    if ((st = build_metadata(p, ms, nullptr, meas_slot0)) != CUI_OK) return st;
+    if ((st = select_device_and_shapes(p, d->device)) != CUI_OK) return st;
+
+    std::vector<float2> T;
+    if ((st = build_table(p, d, T)) != CUI_OK) return st;
+    CUI_TRY(upload(p, &p.table, T));
+    p.table_bytes = T.size() * sizeof(float2);
+    std::vector<float2>().swap(T);
     std::vector<float2> pin(static_cast<size_t>(p.S) * p.P);
     for (int w = 0; w < p.W; ++w) {
         const cui_measurement_desc& m = d->measurements[w];
@@ -316,42 +414,12 @@ cui_status create(const cui_born_desc* d, int32_t max_objects, Plan& p) {
                 pin[static_cast<size_t>(meas_slot0[w] + k) * p.P + pt] = to_f2(c);
             }
     }
-
-#define CUI_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return check_cuda(e_, #x); } while (0)
-    CUI_TRY(upload(p, &p.table, T));
     CUI_TRY(upload(p, &p.p_in, pin));
-    p.table_bytes = T.size() * sizeof(float2);
     p.incident_bytes = pin.size() * sizeof(float2);
-    std::vector<float2>().swap(T);
     std::vector<float2>().swap(pin);
-    CUI_TRY(upload(p, &p.f_slot_ptr, f_slot_ptr));
-    CUI_TRY(upload(p, &p.f_slot_list, f_slot_list));
-    CUI_TRY(upload(p, &p.row_slot, row_slot));
-    CUI_TRY(upload(p, &p.row_mix, row_mix));
-    CUI_TRY(upload(p, &p.row_fl, row_fl));
-    CUI_TRY(upload(p, &p.mix_nact, mix_nact));
-    CUI_TRY(upload(p, &p.mix_nf, mix_nf));
-    CUI_TRY(upload(p, &p.mix_pref_off, mix_pref_off));
-    CUI_TRY(upload(p, &p.mix_act_off, mix_act_off));
-    CUI_TRY(upload(p, &p.act, act));
-    CUI_TRY(upload(p, &p.pref, pref));
-    CUI_TRY(upload(p, &p.pos, pos));
-    CUI_TRY(upload(p, &p.slot_row_ptr, slot_row_ptr));
-    CUI_TRY(upload(p, &p.slot_rows, slot_rows));
-
-    const size_t part_fwd = static_cast<size_t>(p.fwd_groups) * p.S * max_objects * p.E;
-    const size_t part_adj = static_cast<size_t>(p.adj_nfc) * max_objects * p.P;
-    p.ws_part_bytes = std::max(part_fwd, part_adj) * sizeof(float2);
-    CUI_TRY(dalloc(p, &p.ws_part, std::max(part_fwd, part_adj)));
-    CUI_TRY(dalloc(p, &p.ws_G, static_cast<size_t>(p.S) * max_objects * p.E));
-    CUI_TRY(dalloc(p, &p.ws_r, static_cast<size_t>(p.n_obs) * max_objects));
-    CUI_TRY(dalloc(p, &p.ws_loss, loss_workspace_floats(max_objects)));
-    p.workspace_bytes = p.ws_part_bytes + sizeof(float2) * (static_cast<size_t>(p.S) * max_objects * p.E +
-                                                            static_cast<size_t>(p.n_obs) * max_objects) +
-                        sizeof(float) * loss_workspace_floats(max_objects);
-#undef CUI_TRY
-    return CUI_OK;
+    return upload_metadata_and_workspace(p);
 }
+#undef CUI_TRY
 
 bool valid_plan(const cui_born_plan* plan) { return plan != nullptr; }
 
@@ -453,6 +521,35 @@ cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t
     return cui::vjp_device(&plan->p, reinterpret_cast<const float2*>(gamma), ld_gamma,
                            reinterpret_cast<const float2*>(u_meas), ld_u, n_objects, reinterpret_cast<float2*>(grad),
                            ld_grad, loss, static_cast<cudaStream_t>(stream));
+}
+
+cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable) {
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    plan->p.timing = enable != 0;
+    return CUI_OK;
+}
+
+cui_status cui_born_timing_read(cui_born_plan* plan, cui_born_timing* out) {
+    if (!plan || !out) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
+    cui::Plan& p = plan->p;
+    *out = cui_born_timing{0, 0, 0.0, 0.0};
+    cudaSetDevice(p.device);
+    for (size_t i = 0; i < p.ev_used; ++i) {
+        cudaError_t e = cudaEventSynchronize(p.ev_pool[2 * i + 1]);
+        if (e != cudaSuccess) return cui::check_cuda(e, "cudaEventSynchronize");
+        float ms = 0.f;
+        if ((e = cudaEventElapsedTime(&ms, p.ev_pool[2 * i], p.ev_pool[2 * i + 1])) != cudaSuccess)
+            return cui::check_cuda(e, "cudaEventElapsedTime");
+        if (p.ev_kind[i] == 0) {
+            out->n_forward++;
+            out->ms_forward += ms;
+        } else {
+            out->n_adjoint++;
+            out->ms_adjoint += ms;
+        }
+    }
+    p.ev_used = 0;
+    return CUI_OK;
 }
 
 const char* cui_status_string(cui_status status) {

@@ -1,0 +1,416 @@
+// Device-side construction of the operator's tables from physical parameters.
+//
+// The reference computes its tables once per operator on the host in FP64
+// (+scattering/operator.m:76-88): the reference element's transfer function
+// (+scattering/+sequences/+setups/setup.m:1216-1281 with the Green's function
+// of +processing/greens_function.m:88/103 and the anti-aliasing window of
+// +scattering/+anti_aliasing_filters/on.m:64-70, raised_cosine.m:106-119), the
+// incident fields (+scattering/+sequences/sequence.m:813-844) and the
+// prefactors (setup.m:759, sequence.m:623).  cui_born_plan_create_setup does
+// the same on the GPU:
+//   * the lateral-offset table in FP64 arithmetic (one thread per entry),
+//     stored in FP32; the 2D Green's function needs H0^(2) of a complex
+//     argument, evaluated here from its power series (DLMF 10.8.2) for
+//     |z| < 16 and from Hankel's asymptotic expansion (DLMF 10.17.4) above;
+//   * the incident field of every (wave, frequency) as the sum over transmit
+//     elements of table rows shifted by the element offset, weighted by the
+//     normal velocities v_d;
+//   * the prefactors -dV k~(f)^2 times the caller's receive responses.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "cui_internal.cuh"
+
+namespace cui {
+namespace {
+
+// ---- complex FP64 helpers -----------------------------------------------------
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ inline double2 cinv(double2 a) {
+    const double d = a.x * a.x + a.y * a.y;
+    return make_double2(a.x / d, -a.y / d);
+}
+__device__ inline double cabsd(double2 a) { return hypot(a.x, a.y); }
+// principal square root
+__device__ inline double2 csqrt(double2 a) {
+    const double r = hypot(a.x, a.y);
+    double re = sqrt(0.5 * (r + fabs(a.x)));
+    double im = (re > 0.0) ? 0.5 * a.y / re : 0.0;
+    if (a.x < 0.0) {  // rotate into the right half-plane
+        const double t = re;
+        re = fabs(im);
+        im = copysign(t, a.y);
+    }
+    return make_double2(re, im);
+}
+// exp(-i z) for z = x + i y  ->  exp(y) (cos x - i sin x)
+__device__ inline double2 cexp_minus_i(double2 z) {
+    double s, c;
+    sincos(z.x, &s, &c);
+    const double m = exp(z.y);
+    return make_double2(m * c, -m * s);
+}
+__device__ inline double2 clog(double2 z) { return make_double2(log(hypot(z.x, z.y)), atan2(z.y, z.x)); }
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEulerGamma = 0.57721566490153286061;
+constexpr double kHankelSwitch = 16.0;
+
+// H0^(2)(z) for Re z > 0, Im z <= 0 (absorbing media).
+__device__ double2 hankel2_0(double2 z) {
+    if (cabsd(z) >= kHankelSwitch) {
+        // DLMF 10.17.4: H0^(2)(z) ~ sqrt(2/(pi z)) exp(-i(z - pi/4)) sum_k (-i)^k a_k(0) / z^k,
+        // a_k(0)/a_{k-1}(0) = -(2k-1)^2/(8k); the sum is truncated at its smallest term.
+        const double2 w = cinv(z);
+        double2 term = make_double2(1.0, 0.0), sum = term;
+        double prev = 1.0;
+        for (int k = 1; k < 64; ++k) {
+            const double c = (2.0 * k - 1.0) * (2.0 * k - 1.0) / (8.0 * k);
+            const double2 next = cmul(cmul(term, make_double2(0.0, c)), w);  // * (-i) * (-(2k-1)^2/(8k)) / z
+            const double mag = cabsd(next);
+            if (mag >= prev) break;
+            term = next;
+            sum = cadd(sum, term);
+            prev = mag;
+            if (mag < 1e-17 * cabsd(sum)) break;
+        }
+        const double2 pre = csqrt(cscale(cinv(z), 2.0 / kPi));
+        const double2 ph = cmul(cexp_minus_i(z), make_double2(0.70710678118654752440, 0.70710678118654752440));
+        return cmul(cmul(pre, ph), sum);
+    }
+    // DLMF 10.2.2 / 10.8.2: J0 = sum (-q)^k/(k!)^2, Y0 = (2/pi)(ln(z/2)+gamma) J0 + (2/pi) sum_{k>=1} (-1)^{k+1} H_k q^k/(k!)^2,
+    // q = z^2/4, H_k the harmonic numbers; H0^(2) = J0 - i Y0.
+    const double2 q = cscale(cmul(z, z), 0.25);
+    double2 t = make_double2(1.0, 0.0), J = t, Ys = make_double2(0.0, 0.0);
+    double H = 0.0;
+    for (int k = 1; k < 80; ++k) {
+        t = cscale(cmul(t, make_double2(-q.x, -q.y)), 1.0 / (static_cast<double>(k) * k));
+        H += 1.0 / k;
+        J = cadd(J, t);
+        Ys = cadd(Ys, cscale(t, -H));
+        if (k > 4 && cabsd(t) < 1e-18 * cabsd(J)) break;
+    }
+    const double2 L = clog(cscale(z, 0.5));
+    const double2 Y = cadd(cscale(cmul(make_double2(L.x + kEulerGamma, L.y), J), 2.0 / kPi), cscale(Ys, 2.0 / kPi));
+    return make_double2(J.x + Y.y, J.y - Y.x);  // J - i Y
+}
+
+__device__ inline double raised_cosine(double flag, double beta) {
+    const double lb = kPi * (1.0 - beta);
+    if (flag <= lb) return 1.0;
+    if (flag >= kPi) return 0.0;
+    return 0.5 * (1.0 + cos(kPi * (flag - lb) / (kPi - lb)));
+}
+
+struct TableArgs {
+    int n_dims, F, Nz, Noy, Nox, Ex, Ey, Qx, Qy;
+    double dx, dy, dz, z_start, pitch_x, pitch_y, wx, wy, dA, beta;
+    const double2* k;   // [F]
+    float2* out;        // [F][Nz][Noy][Nox]
+    int* bad;           // set when an entry is not finite
+};
+
+// one thread per entry (f, z, oy, ox); FP64 arithmetic, FP32 store
+__global__ void table_kernel(const TableArgs a) {
+    const int64_t n = static_cast<int64_t>(a.F) * a.Nz * a.Noy * a.Nox;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int ox = static_cast<int>(i % a.Nox);
+        int64_t t = i / a.Nox;
+        const int oy = static_cast<int>(t % a.Noy);
+        t /= a.Noy;
+        const int z = static_cast<int>(t % a.Nz);
+        const int f = static_cast<int>(t / a.Nz);
+        const double X = (ox - 0.5 * (a.Nox - 1)) * a.dx;
+        const double Y = (a.n_dims == 3) ? (oy - 0.5 * (a.Noy - 1)) * a.dy : 0.0;
+        const double Z = a.z_start + (z + 0.5) * a.dz;
+        const double2 k = a.k[f];
+        double2 sum = make_double2(0.0, 0.0);
+        for (int qy = 0; qy < a.Qy; ++qy) {
+            const double fy = (a.n_dims == 3) ? (qy - 0.5 * (a.Qy - 1)) * (a.wy / a.Qy) : 0.0;
+            for (int qx = 0; qx < a.Qx; ++qx) {
+                const double fx = (qx - 0.5 * (a.Qx - 1)) * (a.wx / a.Qx);
+                const double D = sqrt((X - fx) * (X - fx) + (Y - fy) * (Y - fy) + Z * Z);
+                const double2 kD = cscale(k, D);
+                double2 G;
+                if (a.n_dims == 2) {
+                    const double2 h = hankel2_0(kD);
+                    G = make_double2(-0.25 * h.y, 0.25 * h.x);             // 0.25j * H0^(2)(kD)
+                } else {
+                    G = cscale(cexp_minus_i(kD), -1.0 / (4.0 * kPi * D));  // -exp(-j k D)/(4 pi D)
+                }
+                sum = cadd(sum, G);
+            }
+        }
+        double w = 1.0;
+        if (a.beta >= 0.0) {
+            const double dist = sqrt(X * X + Y * Y + Z * Z);
+            if (a.Ex > 1) w *= raised_cosine(k.x * a.pitch_x * fabs(X) / dist, a.beta);
+            if (a.n_dims == 3 && a.Ey > 1) w *= raised_cosine(k.x * a.pitch_y * fabs(Y) / dist, a.beta);
+        }
+        const double2 v = cscale(sum, -2.0 * a.dA * w);
+        if (!isfinite(v.x) || !isfinite(v.y)) *a.bad = 1;
+        a.out[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    }
+}
+
+struct PinArgs {
+    int Nx, Ny, Nz, Ex, Ey, ppx, ppy, Nox, Noy;
+    int64_t P;
+    const float2* table;   // transmit table [F][Nz][Noy][Nox]
+    const float2* vd;      // [S][E]
+    const int* slot_f;     // [S]
+    float2* p_in;          // [S][P]
+};
+
+// p_in[s][p] = sum_e T_tx[f_s][z][o(p, e)] * v_d[s][e]; block = (line, slot, x chunk), thread = x
+__global__ void __launch_bounds__(256) incident_kernel(const PinArgs a) {
+    extern __shared__ float2 sm[];
+    float2* srow = sm;             // [Nox]
+    float2* svd = sm + a.Nox;      // [Ex]
+    const int line = blockIdx.x, s = blockIdx.y;
+    const int iy = line % a.Ny, z = line / a.Ny;
+    const int f = a.slot_f[s];
+    const int64_t pt0 = (static_cast<int64_t>(z) * a.Ny + iy) * a.Nx;
+    const int x = blockIdx.z * blockDim.x + threadIdx.x;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int ey = 0; ey < a.Ey; ++ey) {
+        const int oy = iy - ey * a.ppy + (a.Ey - 1) * a.ppy;
+        const float2* row = a.table + ((static_cast<int64_t>(f) * a.Nz + z) * a.Noy + oy) * a.Nox;
+        __syncthreads();
+        for (int i = threadIdx.x; i < a.Nox; i += blockDim.x) srow[i] = row[i];
+        for (int i = threadIdx.x; i < a.Ex; i += blockDim.x) svd[i] = a.vd[static_cast<int64_t>(s) * a.Ex * a.Ey + i + a.Ex * ey];
+        __syncthreads();
+        if (x < a.Nx) {
+            const int o0 = x + (a.Ex - 1) * a.ppx;
+            for (int ex = 0; ex < a.Ex; ++ex) {
+                const float2 h = srow[o0 - ex * a.ppx];
+                const float2 v = svd[ex];
+                acc.x = fmaf(h.x, v.x, fmaf(-h.y, v.y, acc.x));
+                acc.y = fmaf(h.x, v.y, fmaf(h.y, v.x, acc.y));
+            }
+        }
+    }
+    if (x < a.Nx) a.p_in[static_cast<int64_t>(s) * a.P + pt0 + x] = acc;
+}
+
+// complex wavenumbers k~(f): +scattering/+sequences/+setups/+materials/+absorption_models/
+// none.m:83 and time_causal.m:82-83, :118-147
+std::vector<double2> wavenumbers(const cui_absorption_desc& a, const double* f, int F, cui_status* st) {
+    std::vector<double2> k(F);
+    *st = CUI_OK;
+    if (!(a.c > 0.0)) {
+        *st = set_error(CUI_ERR_INVALID_ARG, "absorption.c must be positive");
+        return k;
+    }
+    if (a.kind == CUI_ABSORPTION_NONE) {
+        for (int i = 0; i < F; ++i) k[i] = make_double2(2.0 * kPi * f[i] / a.c, 0.0);
+        return k;
+    }
+    if (a.kind != CUI_ABSORPTION_TIME_CAUSAL) {
+        *st = set_error(CUI_ERR_INVALID_ARG, "unknown absorption model");
+        return k;
+    }
+    const double alpha_0 = a.constant_db * std::log(10.0) / (20.0 * 0.01);
+    const double alpha_1 = a.slope_db * std::log(10.0) / (20.0 * 0.01 * std::pow(1e6, a.exponent));
+    const double y = a.exponent;
+    for (int i = 0; i < F; ++i) {
+        const double fi = f[i];
+        const double k_ref = 2.0 * kPi * fi / a.c;
+        const double k_imag = -alpha_0 - alpha_1 * std::pow(std::fabs(fi), y);
+        double k_real = k_ref;
+        if (a.dispersion) {
+            if (std::fmod(y, 2.0) == 0.0 || std::floor(y) != y)
+                k_real = k_ref + alpha_1 * std::tan(y * kPi / 2.0) * fi *
+                                     (std::pow(std::fabs(fi), y - 1.0) - std::pow(std::fabs(a.f_ref), y - 1.0));
+            else
+                k_real = k_ref - 2.0 * alpha_1 * std::pow(fi, y) * std::log(std::fabs(fi / a.f_ref)) / kPi;
+        }
+        if (std::fabs(fi) < 2.220446049250313e-16) k_real = 0.0;
+        k[i] = make_double2(k_real, k_imag);
+    }
+    return k;
+}
+
+int points_per_pitch(double pitch, double delta, bool* ok) {
+    const double r = pitch / delta;
+    const double n = std::round(r);
+    *ok = (n >= 1.0) && std::fabs(r - n) <= 1e-9 * n;
+    return static_cast<int>(n);
+}
+
+#define CUI_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return check_cuda(e_, #x); } while (0)
+
+cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk, double beta, float2* out, int* dbad) {
+    TableArgs a;
+    a.n_dims = p.n_dims; a.F = p.F; a.Nz = p.Nz; a.Noy = p.Noy; a.Nox = p.Nox; a.Ex = p.Ex; a.Ey = p.Ey;
+    a.Qx = std::max(1, d->n_face_axis[0]);
+    a.Qy = (p.n_dims == 3) ? std::max(1, d->n_face_axis[1]) : 1;
+    a.dx = d->delta_axis[0];
+    a.dy = (p.n_dims == 3) ? d->delta_axis[1] : 0.0;
+    a.dz = d->delta_axis[p.n_dims - 1];
+    a.z_start = d->z_start;
+    a.pitch_x = d->pitch_axis[0];
+    a.pitch_y = (p.n_dims == 3) ? d->pitch_axis[1] : 0.0;
+    a.wx = d->width_axis[0];
+    a.wy = (p.n_dims == 3) ? d->width_axis[1] : 0.0;
+    a.dA = (a.wx / a.Qx) * ((p.n_dims == 3) ? a.wy / a.Qy : 1.0);
+    a.beta = beta;
+    a.k = dk;
+    a.out = out;
+    a.bad = dbad;
+    const int64_t n = static_cast<int64_t>(p.F) * p.Nz * p.Noy * p.Nox;
+    const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, 152 * 64));
+    table_kernel<<<blocks, 256>>>(a);
+    count_launch();
+    CUI_TRY(cudaGetLastError());
+    return CUI_OK;
+}
+
+cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan& p) {
+    if (!d) return set_error(CUI_ERR_INVALID_ARG, "desc is NULL");
+    if (d->n_dims != 2 && d->n_dims != 3) return set_error(CUI_ERR_INVALID_ARG, "n_dims must be 2 or 3");
+    const int nl = d->n_dims - 1;
+    int32_t ppp[2] = {1, 1};
+    for (int k = 0; k < nl; ++k) {
+        if (!(d->delta_axis[k] > 0.0) || !(d->pitch_axis[k] > 0.0) || !(d->width_axis[k] > 0.0))
+            return set_error(CUI_ERR_INVALID_ARG, "delta, pitch and width must be positive");
+        bool ok = false;
+        ppp[k] = points_per_pitch(d->pitch_axis[k], d->delta_axis[k], &ok);
+        if (!ok)
+            return set_error(CUI_ERR_UNSUPPORTED_SETUP,
+                             "element pitch is not an integer multiple of the lateral grid spacing (setup.m:1176-1178)");
+    }
+    if (!(d->delta_axis[nl] > 0.0) || !(d->z_start >= 0.0))
+        return set_error(CUI_ERR_INVALID_ARG, "axial spacing must be positive and z_start non-negative");
+    if (!d->f_unique || !d->waves) return set_error(CUI_ERR_INVALID_ARG, "f_unique or waves is NULL");
+    cui_status st = init_geometry(p, d->n_dims, d->n_points_axis, d->n_elements_axis, ppp, d->n_f_unique,
+                                  d->n_measurements, max_objects);
+    if (st != CUI_OK) return st;
+    std::vector<double2> k = wavenumbers(d->absorption, d->f_unique, p.F, &st);
+    if (st != CUI_OK) return st;
+    double dV = 1.0;
+    for (int a = 0; a < d->n_dims; ++a) dV *= d->delta_axis[a];
+    std::vector<double2> scale(p.F);
+    for (int f = 0; f < p.F; ++f) scale[f] = cscale(cmul(k[f], k[f]), -dV);  // -dV k~^2 (setup.m:759)
+    std::vector<MeasIn> ms(p.W);
+    for (int w = 0; w < p.W; ++w) {
+        const cui_wave_desc& wd = d->waves[w];
+        if (!wd.v_d) return set_error(CUI_ERR_INVALID_ARG, "wave " + std::to_string(w) + " has no v_d");
+        ms[w] = MeasIn{wd.n_f, wd.indices_f_to_unique, wd.n_mixes, wd.mixes};
+    }
+    std::vector<int> slot0;
+    if ((st = build_metadata(p, ms, &scale, slot0)) != CUI_OK) return st;
+    if ((st = select_device_and_shapes(p, d->device)) != CUI_OK) return st;
+
+    // v_d of every slot, FP32 [S][E]
+    std::vector<float2> vd(static_cast<size_t>(p.S) * p.E);
+    for (int w = 0; w < p.W; ++w) {
+        const cui_wave_desc& wd = d->waves[w];
+        for (int e = 0; e < p.E; ++e)
+            for (int i = 0; i < wd.n_f; ++i) {
+                const cui_complex64 c = wd.v_d[static_cast<int64_t>(e) * wd.n_f + i];
+                if (!std::isfinite(c.re) || !std::isfinite(c.im)) return set_error(CUI_ERR_NUMERIC, "non-finite v_d");
+                vd[static_cast<size_t>(slot0[w] + i) * p.E + e] = make_float2(static_cast<float>(c.re), static_cast<float>(c.im));
+            }
+    }
+
+    // scratch for the build (released before returning)
+    double2* dk = nullptr;
+    float2* dvd = nullptr;
+    int* dslot = nullptr;
+    int* dbad = nullptr;
+    float2* dtx = nullptr;
+    std::vector<void*> tmp;
+    auto release = [&]() {
+        for (void* v : tmp) cudaFree(v);
+        tmp.clear();
+    };
+    auto talloc = [&](void** ptr, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(ptr, std::max<size_t>(bytes, 1));
+        if (e == cudaSuccess) tmp.push_back(*ptr);
+        return e;
+    };
+    cudaError_t ce;
+    const size_t tbytes = sizeof(float2) * static_cast<size_t>(p.F) * p.Nz * p.Noy * p.Nox;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.table), tbytes)) != CUI_OK) return st;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_in), sizeof(float2) * static_cast<size_t>(p.S) * p.P)) != CUI_OK)
+        return st;
+    p.table_bytes = tbytes;
+    p.incident_bytes = sizeof(float2) * static_cast<size_t>(p.S) * p.P;
+    const bool same_filter = (d->aa_tx_beta < 0.0 && d->aa_rx_beta < 0.0) || (d->aa_tx_beta == d->aa_rx_beta);
+    if ((ce = talloc(reinterpret_cast<void**>(&dk), sizeof(double2) * p.F)) != cudaSuccess ||
+        (ce = talloc(reinterpret_cast<void**>(&dvd), sizeof(float2) * vd.size())) != cudaSuccess ||
+        (ce = talloc(reinterpret_cast<void**>(&dslot), sizeof(int) * p.S)) != cudaSuccess ||
+        (ce = talloc(reinterpret_cast<void**>(&dbad), sizeof(int))) != cudaSuccess ||
+        (!same_filter && (ce = talloc(reinterpret_cast<void**>(&dtx), tbytes)) != cudaSuccess)) {
+        release();
+        return check_cuda(ce, "table build scratch");
+    }
+    if ((ce = cudaMemcpy(dk, k.data(), sizeof(double2) * p.F, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (ce = cudaMemcpy(dvd, vd.data(), sizeof(float2) * vd.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (ce = cudaMemcpy(dslot, p.h_slot_f.data(), sizeof(int) * p.S, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (ce = cudaMemset(dbad, 0, sizeof(int))) != cudaSuccess) {
+        release();
+        return check_cuda(ce, "table build upload");
+    }
+    std::vector<float2>().swap(vd);
+    st = launch_table(p, d, dk, d->aa_rx_beta, p.table, dbad);
+    if (st == CUI_OK && !same_filter) st = launch_table(p, d, dk, d->aa_tx_beta, dtx, dbad);
+    if (st == CUI_OK) {
+        PinArgs a;
+        a.Nx = p.Nx; a.Ny = p.Ny; a.Nz = p.Nz; a.Ex = p.Ex; a.Ey = p.Ey; a.ppx = p.ppx; a.ppy = p.ppy;
+        a.Nox = p.Nox; a.Noy = p.Noy; a.P = p.P;
+        a.table = same_filter ? p.table : dtx;
+        a.vd = dvd; a.slot_f = dslot; a.p_in = p.p_in;
+        const size_t smem = sizeof(float2) * (p.Nox + p.Ex);
+        const int tpb = 256;
+        dim3 grid(p.Ny * p.Nz, p.S, (p.Nx + tpb - 1) / tpb);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(incident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        incident_kernel<<<grid, tpb, smem>>>(a);
+        count_launch();
+        if ((ce = cudaGetLastError()) != cudaSuccess) st = check_cuda(ce, "incident field");
+    }
+    int bad = 0;
+    if (st == CUI_OK) {
+        if ((ce = cudaMemcpy(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            st = check_cuda(ce, "table build");
+        else if (bad)
+            st = set_error(CUI_ERR_NUMERIC, "non-finite transfer-function table entry");
+    }
+    release();
+    if (st != CUI_OK) return st;
+    return upload_metadata_and_workspace(p);
+}
+#undef CUI_TRY
+
+}  // namespace
+}  // namespace cui
+
+extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
+                                                 cui_born_plan** plan) {
+    if (!plan) return cui::set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    *plan = nullptr;
+    cui_born_plan* h = new (std::nothrow) cui_born_plan();
+    if (!h) return cui::set_error(CUI_ERR_OOM, "host allocation failed");
+    cui_status s;
+    try {
+        s = cui::create_setup(desc, max_objects, h->p);
+    } catch (const std::bad_alloc&) {
+        s = cui::set_error(CUI_ERR_OOM, "host allocation failed");
+    }
+    if (s != CUI_OK) {
+        cui_born_plan_destroy(h);
+        return s;
+    }
+    *plan = h;
+    return CUI_OK;
+}

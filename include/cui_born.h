@@ -116,12 +116,62 @@ typedef struct {
     int64_t contraction_macs;       /* complex MACs of one dense apply per object: sum_slots E*P */
 } cui_born_info;
 
+/* ---- setup form: tables built on the device ---------------------------------
+ * Instead of the precomputed tables, the caller describes the discretised
+ * setup; the plan computes the lateral transfer-function table (FP64
+ * arithmetic, setup.m:1216-1281, greens_function.m:88/103, on.m:64-70,
+ * raised_cosine.m:106-119), the incident fields (sequence.m:813-844) and the
+ * prefactors -dV k~^2 R (setup.m:759, sequence.m:623) on the GPU. */
+typedef enum { CUI_ABSORPTION_NONE = 0, CUI_ABSORPTION_TIME_CAUSAL = 1 } cui_absorption_kind;
+
+typedef struct {
+    int32_t kind;          /* cui_absorption_kind */
+    double c;              /* none: c_0; time_causal: c_ref (m/s) */
+    double constant_db;    /* time_causal: absorption constant (dB/cm), time_causal.m:82 */
+    double slope_db;       /* time_causal: slope (dB/(MHz^y cm)), time_causal.m:83 */
+    double exponent;       /* time_causal: y */
+    double f_ref;          /* time_causal: reference frequency (Hz) */
+    int32_t dispersion;    /* time_causal: nonzero = causal dispersion, time_causal.m:124-136 */
+} cui_absorption_desc;
+
+/* One incident wave (sequential pulse-echo measurement) of the setup form. */
+typedef struct {
+    int32_t n_f;                          /* unique frequencies of the wave */
+    const int32_t* indices_f_to_unique;   /* [n_f] 1-based into f_unique */
+    const cui_complex64* v_d;             /* [n_f x N_elements] column-major normal velocities
+                                             (settings(m).v_d_unique, tx.m:284; zero = inactive) */
+    int32_t n_mixes;
+    const cui_mix_desc* mixes;            /* here `prefactors` holds the receive responses R
+                                             (DFT of the mixer impulse responses); the plan
+                                             multiplies them by -dV k~(f)^2 */
+} cui_wave_desc;
+
+typedef struct {
+    int32_t n_dims;                 /* 2 or 3 */
+    int32_t n_points_axis[3];       /* FOV grid points: lateral axes then axial */
+    double delta_axis[3];           /* FOV grid spacing (m) */
+    double z_start;                 /* axial position of the FOV's near edge (m); rows at z_start + (k+1/2) dz */
+    int32_t n_elements_axis[2];
+    double pitch_axis[2];           /* element pitch (m); must be an integer multiple of the lateral spacing */
+    double width_axis[2];           /* element face width (m) */
+    int32_t n_face_axis[2];         /* quadrature points across each face axis */
+    cui_absorption_desc absorption;
+    double aa_tx_beta, aa_rx_beta;  /* raised-cosine roll-off of the anti-aliasing filters; < 0 = off */
+    int32_t n_f_unique;
+    const double* f_unique;         /* [n_f_unique] global unique frequencies (Hz) */
+    int32_t n_measurements;
+    const cui_wave_desc* waves;
+    int32_t device;
+} cui_born_setup_desc;
+
 /* ---- plan lifetime ------------------------------------------------------ */
 /* Validates the descriptor, converts every table to FP32 in the device
  * layout and uploads it.  Replaces the per-call host conversion and uploads
  * of .cu:520-850.  `max_objects` bounds the number of columns of one apply
  * (it sizes the plan's workspace). */
 cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, cui_born_plan** plan);
+/* Same plan from the setup form (tables computed on the device). */
+cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects, cui_born_plan** plan);
 cui_status cui_born_plan_destroy(cui_born_plan* plan);
 cui_status cui_born_plan_info(const cui_born_plan* plan, cui_born_info* info);
 
@@ -162,6 +212,19 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
                              cui_complex64* grad, int64_t ld_grad, double* loss);
 
 /* ---- diagnostics ----------------------------------------------------------- */
+/* Device time of the two contraction kernels, from CUDA events recorded on
+ * the launching stream around each launch while timing is enabled. */
+typedef struct {
+    int64_t n_forward;      /* forward contraction launches since the last read */
+    int64_t n_adjoint;      /* adjoint contraction launches since the last read */
+    double ms_forward;      /* summed device time of those launches (ms) */
+    double ms_adjoint;
+} cui_born_timing;
+
+cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable);
+/* Waits for the recorded events, returns the sums and clears them. */
+cui_status cui_born_timing_read(cui_born_plan* plan, cui_born_timing* out);
+
 const char* cui_status_string(cui_status status);
 /* Message of the last failing call on this thread (empty if none). */
 const char* cui_last_error(void);

@@ -160,6 +160,22 @@ def mix_weights(cfg: BornConfig):
     return np.where(rng.random((cfg.n_mixes, E)) < 0.5, -1.0, 1.0)
 
 
+def mix_layout(cfg: BornConfig, n_f_wave: int):
+    """Per mix: (frequency indices into the wave's frequencies, active elements,
+    receive responses R (F_mix, n_active))."""
+    weights = mix_weights(cfg)
+    out = []
+    for m in range(weights.shape[0]):
+        active = np.nonzero(weights[m])[0]
+        if cfg.mix_f_stride > 1:
+            mf = np.arange(m % 2, n_f_wave, cfg.mix_f_stride)
+        else:
+            mf = np.arange(n_f_wave)
+        resp = np.repeat(weights[m, active][None, :], len(mf), axis=0).astype(np.complex128)
+        out.append((mf, active, resp))
+    return out
+
+
 @dataclasses.dataclass
 class BuiltOperator:
     """Oracle tables plus the lateral-offset form consumed by the CUDA path."""
@@ -211,15 +227,10 @@ def build(cfg: BornConfig, direct_elements: bool = False) -> BuiltOperator:
         v_d = wave_vd(cfg, wave, fw)
         p_in = incident_field(s, fw, v_d, lambda e: element_from_table(s, T_tx, e)[f_idx])
         mixes = []
-        for m in range(weights.shape[0]):
-            active = np.nonzero(weights[m])[0]
-            mf = np.arange(0, len(f_idx), cfg.mix_f_stride) if cfg.mix_f_stride > 1 else np.arange(len(f_idx))
-            if cfg.mix_f_stride > 1 and m % 2 == 1:
-                mf = np.arange(1, len(f_idx), cfg.mix_f_stride)
+        for mf, active, resp in mix_layout(cfg, len(f_idx)):
             kk = k[f_idx[mf]]
             # prefactors -dV k~^2 (setup.m:759) times the receive impulse-response DFT (sequence.m:623)
-            pref = (-s.cell_volume * kk ** 2)[:, None] * weights[m, active][None, :].astype(np.complex128)
-            mixes.append(Mix(f_idx=mf, active=active, pref=pref))
+            mixes.append(Mix(f_idx=mf, active=active, pref=(-s.cell_volume * kk ** 2)[:, None] * resp))
         measurements.append(Measurement(f_idx=f_idx, p_incident=p_in, mixes=mixes))
     shift, valid = shift_lateral(s)
     op = OperatorTables(setup=s, f_unique=f, measurements=measurements)

@@ -1,0 +1,106 @@
+"""Timed CPU baseline: the FP64 oracle operator on a bounded sample of a workload.
+
+TEST/BENCH INFRASTRUCTURE ONLY: used by ``bench.py``'s ``cpu_baseline`` leg
+and by ``bench.py --impl reference``.  The reference's own CPU operator
+(MATLAB ``forward_quick_cpu`` / ``adjoint_quick_cpu``) cannot run on these
+machines; its restatement in :mod:`oracle.born_oracle` keeps the same loop
+structure (per measurement, mix and active element: gather the shifted
+transfer function, form Phi = h .* p_in .* pref, multiply with BLAS), and
+that is what is timed here.
+
+The sample keeps the full grid and every element but only ``n_waves`` waves
+and ``n_freq`` frequencies; the work of the operator is linear in
+(waves x frequencies), so the full-workload rate is the sample rate divided
+by ``(S_full / S_sample)``.  Mixes are split over a ``spawn`` process pool,
+one worker per host core; each worker builds the sample's tables itself
+(untimed) and the timed region covers the forward and adjoint applies.
+"""
+
+from __future__ import annotations
+
+import multiprocessing as mp
+import os
+import time
+
+import numpy as np
+
+_STATE = {}
+
+
+def _sample_config(name: str, n_waves: int, n_freq: int):
+    from oracle import configs
+    cfg = configs.config(name)
+    f_idx = np.linspace(0, len(cfg.f) - 1, n_freq).round().astype(int)
+    cfg.f = cfg.f[f_idx]
+    cfg.waves = cfg.waves[:n_waves]
+    return cfg
+
+
+def _init(name, n_waves, n_freq, seed):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import configs
+    cfg = _sample_config(name, n_waves, n_freq)
+    b = configs.build(cfg)
+    rng = np.random.default_rng(seed)
+    P = cfg.setup.n_points
+    gamma = rng.standard_normal((P, 1))
+    _STATE.update(b=b, gamma=gamma)
+
+
+def _work(args):
+    """Forward and adjoint restricted to a chunk of mixes of every measurement."""
+    import dataclasses
+    from oracle import adjoint_quick_cpu, forward_quick_cpu
+    lo, hi = args
+    if hi <= lo:  # warm-up call: the initializer has built the tables
+        return 0.0, 0.0
+    b = _STATE["b"]
+    meas = [dataclasses.replace(m, mixes=m.mixes[lo:hi]) for m in b.op.measurements]
+    op = dataclasses.replace(b.op, measurements=meas)
+    t0 = time.perf_counter()
+    u = forward_quick_cpu(op, _STATE["gamma"])
+    g = adjoint_quick_cpu(op, u)
+    return time.perf_counter() - t0, float(np.abs(g).sum())
+
+
+def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: int | None = None,
+                repeats: int = 1, seed: int = 0):
+    """Seconds per forward+adjoint apply of the full workload, extrapolated from a sample.
+
+    Returns a dict with the sample description, the measured seconds and the
+    extrapolated full-workload applies/s.
+    """
+    from oracle import configs
+    full = configs.config(name)
+    S_full = len(full.waves) * len(full.f)
+    S_sample = n_waves * n_freq
+    n_mix = full.setup.n_elements if full.mixing == "identity" else full.n_mixes
+    procs = processes or os.cpu_count() or 1
+    procs = max(1, min(procs, n_mix))
+    bounds = np.linspace(0, n_mix, procs + 1).round().astype(int)
+    chunks = [(int(bounds[i]), int(bounds[i + 1])) for i in range(procs)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed)) as pool:
+        pool.map(_work, [(0, 0)] * procs)  # wait until every worker holds its tables
+        times = []
+        for _ in range(repeats):
+            # critical path of the parallel apply: the slowest worker's own compute time
+            times.append(max(t for t, _ in pool.map(_work, chunks, chunksize=1)))
+    t_sample = min(times)
+    t_full = t_sample * S_full / S_sample
+    return {
+        "seconds_sample": t_sample,
+        "seconds_full_apply": t_full,
+        "applies_per_s": 1.0 / t_full,
+        "cores": procs,
+        "sample": f"{n_waves} of {len(full.waves)} waves x {n_freq} of {len(full.f)} frequencies, full "
+                  f"{'x'.join(map(str, full.setup.n_points_axis))} grid, all {full.setup.n_elements} elements; "
+                  f"one forward + one adjoint (FP64 numpy/scipy restatement of forward_quick_cpu/adjoint_quick_cpu), "
+                  f"mixes split over {procs} spawn processes; full-workload rate = sample rate x {S_sample}/{S_full}",
+    }
+
+
+if __name__ == "__main__":
+    import json
+    print(json.dumps(time_sample()))

@@ -230,3 +230,34 @@ def test_native_kernels_launched():
     op.forward(dev(configs.make_gamma(b.cfg)))
     torch.cuda.synchronize()
     assert launch_count() - n0 >= 3
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_setup_form_tables_built_on_device(name):
+    """Tables computed on the GPU (FP64 Green's functions, FP32 storage) give the oracle's operator."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from tests.helpers import setup_kwargs
+    b = built(name)
+    B = b.cfg.n_objects
+    op = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B)
+    assert op.size == (b.op.n_observations, b.cfg.setup.n_points)
+    gamma = configs.make_gamma(b.cfg)
+    assert rel_l2(op.forward(dev(gamma)).cpu().numpy(), forward_quick_cpu(b.op, gamma)) <= TOL
+    y = rand_obs(b, B, 9)
+    assert rel_l2(op.adjoint(dev(y)).cpu().numpy(), adjoint_quick_cpu(b.op, y)) <= TOL
+
+
+def test_setup_form_hankel_small_arguments():
+    """Points close to the array (|k r| < 16) use the power-series branch of H0^(2)."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from oracle import Absorption, Setup
+    from tests.helpers import setup_kwargs
+    s = Setup(n_points_axis=(24, 8), delta_axis=(1e-4, 1e-4), z_start=1e-4, n_elements_axis=(6,),
+              pitch_axis=(2e-4,), width_axis=(1.8e-4,), n_face_axis=(3,),
+              absorption=Absorption("time_causal", 1500.0, 0.0, 0.5, 1.0, 4e6, True))
+    cfg = configs.BornConfig("near-field", s, np.linspace(1e6, 4e6, 5), [configs.Wave("qpw", (10.0,))],
+                             density=0.2, seed=3)
+    b = configs.build(cfg, direct_elements=True)
+    op = OperatorBorn.from_setup(**setup_kwargs(cfg), max_objects=1)
+    gamma = configs.make_gamma(cfg)
+    assert rel_l2(op.forward(dev(gamma)).cpu().numpy(), forward_quick_cpu(b.op, gamma)) <= TOL

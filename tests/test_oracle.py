@@ -147,3 +147,28 @@ def test_golden_fixture_reproduced():
         ref = gold[k]
         np.testing.assert_allclose(now[k], ref, rtol=1e-12, atol=1e-13 * max(1e-300, float(np.max(np.abs(ref)))),
                                    err_msg=k)
+
+
+@pytest.mark.parametrize("wname,cname", [("2d-plain", "c0"), ("2d-gradient", "c1"), ("2d-batched", "c2"),
+                                         ("3d", "c3")])
+def test_benchmark_workloads_match_oracle_configs(wname, cname):
+    """The benchmark's synthetic inputs are the oracle's workloads, value for value."""
+    from comp_ui_toolbox_gb300.workloads import workload
+    w = workload(wname)
+    c = configs.config(cname)
+    s = c.setup
+    assert w.n_points_axis == s.n_points_axis and w.n_elements_axis == s.n_elements_axis
+    np.testing.assert_allclose(w.delta_axis, s.delta_axis, rtol=0)
+    np.testing.assert_allclose(w.pitch_axis, s.pitch_axis, rtol=0)
+    np.testing.assert_allclose(w.width_axis, s.width_axis, rtol=0)
+    assert w.z_start == s.z_start and w.n_face_axis == s.n_face_axis
+    assert w.absorption["kind"] == s.absorption.kind and w.absorption["c"] == s.absorption.c
+    if s.absorption.kind == "time_causal":
+        assert w.absorption["slope_db"] == s.absorption.slope_db and w.absorption["f_ref"] == s.absorption.f_ref
+    np.testing.assert_array_equal(w.f, c.f)
+    assert len(w.waves) == len(c.waves)
+    for ww, cw in zip(w.waves, c.waves):
+        np.testing.assert_allclose(w.wave_vd(ww), configs.wave_vd(c, cw, c.f), rtol=1e-15, atol=1e-15)
+    np.testing.assert_array_equal(w.mix_weights(), configs.mix_weights(c))
+    assert w.n_objects == c.n_objects and w.density == c.density and w.seed == c.seed
+    np.testing.assert_array_equal(w.gamma(n_objects=1), configs.make_gamma(c, n_objects=1))
