@@ -36,12 +36,14 @@ ORACLE_NAME = {"2d-plain": "c0", "2d-gradient": "c1", "2d-batched": "c2", "3d": 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="2d-gradient")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--n-freq", type=int, default=None,
+                    help="keep only the first N frequencies (reduced case for profiler captures)")
     return ap.parse_args()
 
 
@@ -63,7 +65,7 @@ def peaks():
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -71,6 +73,13 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.file = None
+        self.t0 = self.t1 = None
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def __enter__(self):
         try:
@@ -98,16 +107,20 @@ class ClockSampler:
         os.unlink(self.file.name)
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        import datetime
         for r in rows:
             r = [x.strip() for x in r]
-            if len(r) < 9:
+            if len(r) < 10:
                 continue
             try:
-                sm.append(float(r[1]))
-                smax = float(r[2])
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                if self.t0 is not None and not (self.t0 - 0.25 <= ts <= (self.t1 or ts) + 0.25):
+                    continue
+                sm.append(float(r[2]))
+                smax = float(r[3])
             except ValueError:
                 continue
-            for n, v in zip(names, r[5:9]):
+            for n, v in zip(names, r[6:10]):
                 if v.lower() == "active":
                     reasons.add(n)
         sm.sort()
@@ -139,7 +152,6 @@ def run_reference(args):
     w = workload(args.workload)
     B = 1
     from oracle.cpu_baseline import time_sample
-    vals, secs = [], []
     first = time_sample(ORACLE_NAME[args.workload], n_waves=1, n_freq=8, repeats=max(1, args.warmup + args.steps))
     t_full = first["seconds_full_apply"]
     value = first["applies_per_s"]
@@ -150,7 +162,6 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "applies/s", "cores": first["cores"], "kind": "port",
                              "sample": first["sample"]},
             "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    del vals, secs
     print(json.dumps(line), flush=True)
 
 
@@ -167,6 +178,8 @@ def run_ours(args):
     from comp_ui_toolbox_gb300.workloads import workload
 
     w = workload(args.workload)
+    if args.n_freq:
+        w.f = w.f[: args.n_freq]
     B = w.n_objects if args.workload == "2d-batched" else 1
     t0 = time.perf_counter()
     op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=B)
@@ -186,23 +199,25 @@ def run_ours(args):
     def step():
         return op.vjp(gamma, u_meas)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    stream = torch.cuda.current_stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    op.timing(True)
-    op.timing()  # clear
-    n0 = launch_count()
     with ClockSampler(local) as clocks:
+        for _ in range(args.warmup):
+            step()
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        stream = torch.cuda.current_stream()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        op.timing(True)
+        op.timing()  # clear
+        n0 = launch_count()
+        torch.cuda.synchronize()
+        clocks.mark_start()
         ev0.record(stream)
         for _ in range(args.steps):
             grad, loss = step()
         ev1.record(stream)
         torch.cuda.synchronize()
+        clocks.mark_end()
     if world > 1:
         dist.barrier()
     launches = launch_count() - n0

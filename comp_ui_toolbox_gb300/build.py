@@ -19,6 +19,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libcui_born.so"
+HARNESS_SRC = HERE / "harness" / "cui_harness.c"
+HARNESS = HERE / "cui_harness"
 ROOT = HERE.parent
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -48,8 +50,8 @@ def up_to_date() -> bool:
     if not LIB.exists():
         return False
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + list((ROOT / "include").glob("*.h")) + [Path(__file__)]
-    return all(d.stat().st_mtime <= t for d in deps)
+    deps = list(CSRC.glob("*")) + list((ROOT / "include").glob("*.h")) + [Path(__file__), HARNESS_SRC]
+    return HARNESS.exists() and all(d.stat().st_mtime <= t for d in deps)
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
@@ -71,7 +73,18 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
     tmp = LIB.with_suffix(".so.tmp")
     _run([cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
     os.replace(tmp, LIB)
+    build_harness()
     return LIB
+
+
+def build_harness() -> Path:
+    """Plain C driver of the C-ABI (gcc, links libcui_born.so with an $ORIGIN rpath)."""
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if cc is None:
+        raise RuntimeError("no C compiler for the harness")
+    _run([cc, "-O2", "-std=c99", "-Wall", "-Wextra", f"-I{ROOT / 'include'}", str(HARNESS_SRC),
+          f"-L{HERE}", "-lcui_born", "-lm", "-Wl,-rpath,$ORIGIN", "-o", str(HARNESS)])
+    return HARNESS
 
 
 if __name__ == "__main__":

@@ -76,3 +76,9 @@ def test_descriptor_validation_before_any_device_call(lib):
 
 def test_launch_counter_starts_readable(lib):
     assert lib.cui_launch_count() >= 0
+
+
+def test_c_harness_builds_against_the_header(lib):
+    """The plain C driver compiles as C99 against include/cui_born.h and links the library."""
+    from comp_ui_toolbox_gb300 import build
+    assert build.build_harness().exists()

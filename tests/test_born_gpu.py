@@ -261,3 +261,15 @@ def test_setup_form_hankel_small_arguments():
     op = OperatorBorn.from_setup(**setup_kwargs(cfg), max_objects=1)
     gamma = configs.make_gamma(cfg)
     assert rel_l2(op.forward(dev(gamma)).cpu().numpy(), forward_quick_cpu(b.op, gamma)) <= TOL
+
+
+def test_plain_c_harness():
+    """The C-only driver (no Python in the loop) passes its own dot-product and VJP checks."""
+    import json
+    import subprocess
+    from comp_ui_toolbox_gb300 import build
+    exe = build.build_harness()
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    assert res["ok"] and res["dot_product_rel_err"] < 1e-6
