@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <algorithm>
+#include <mutex>
 #include <string>
 
 #include "cui_internal.cuh"
@@ -707,3 +708,118 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
 size_t loss_workspace_floats(int max_objects) { return static_cast<size_t>(kLossBlocks) * max_objects; }
 
 }  // namespace cui
+
+// ---------------------------------------------------------------------------
+// Forward apply that allocates nothing.
+//
+// Some callers cannot call cudaMalloc when they apply the operator: code that
+// runs while a CUDA graph is being captured on the stream (an allocation
+// cannot be captured), hosts that hand their plug-ins a fixed memory budget
+// and forbid further device allocations, and real-time loops that must not
+// touch the allocator between frames.  cui_born_forward_static serves them:
+// it reads the plan's tables like cui_born_forward but keeps its partial sums
+// in a fixed file-scope device array instead of the plan's workspace, and it
+// never allocates.  The array is kStaticScratchBytes large and is held by
+// every GPU that loads the library until the process exits.
+// ---------------------------------------------------------------------------
+namespace cui {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB per device
+static __device__ __align__(256) float2 g_static_scratch[kStaticScratchBytes / sizeof(float2)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+float2* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device.  The name of the
+// array is only a host-side stand-in; kernels need this address.  Looked up
+// once per device, on the first call on that device.
+cudaError_t static_scratch(int device, float2** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_ptr[device] = static_cast<float2*>(p);
+    }
+    *out = g_static_ptr[device];
+    return cudaSuccess;
+}
+
+template <int NC>
+cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, int B, float2* part, int groups,
+                              int lines_per_group, cudaStream_t st) {
+    constexpr int KE = fwd_ke(NC);
+    const FwdShape sh = fwd_shape(p, KE);
+    FwdArgs a;
+    a.g = geom_of(p);
+    a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.lines_per_group = lines_per_group; a.n_lines = p->Ny * p->Nz;
+    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask;
+    a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
+    a.part = part;
+    const size_t smem = fwd_smem_bytes(p, NC);
+    cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    dim3 grid(groups * p->Ey, p->F, B * a.npass);
+    fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace cui
+
+extern "C" cui_status cui_born_forward_static(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
+                                              int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    Plan* p = &plan->p;
+    if (!gamma || !u || n_objects < 1 || ld_gamma < p->P || ld_u < p->n_obs)
+        return set_error(CUI_ERR_INVALID_ARG, "invalid arguments to cui_born_forward_static");
+    // scratch layout: `groups` partial sums [S][B][E] followed by the reduced element signals
+    const size_t slab = sizeof(float2) * static_cast<size_t>(p->S) * n_objects * p->E;
+    if (2 * slab > kStaticScratchBytes)
+        return set_error(CUI_ERR_INVALID_ARG,
+                         "cui_born_forward_static: slots x objects x elements x 16 B exceeds the 16 MiB static "
+                         "scratch; use cui_born_forward or fewer objects per call");
+    const int n_lines = p->Ny * p->Nz;
+    int groups = static_cast<int>(std::min<size_t>(kStaticScratchBytes / slab - 1, static_cast<size_t>(p->fwd_groups)));
+    groups = std::max(1, std::min(groups, n_lines));
+    const int lines_per_group = (n_lines + groups - 1) / groups;
+    groups = (n_lines + lines_per_group - 1) / lines_per_group;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    float2* scratch = nullptr;
+    if ((e = static_scratch(p->device, &scratch)) != cudaSuccess) return check_cuda(e, "cudaGetSymbolAddress");
+    float2* part = scratch;
+    float2* G = scratch + static_cast<size_t>(groups) * p->S * n_objects * p->E;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (pick_nc(p->max_slots_per_f)) {
+        case 1: e = launch_fwd_static<1>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 2: e = launch_fwd_static<2>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 4: e = launch_fwd_static<4>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 8: e = launch_fwd_static<8>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 12: e = launch_fwd_static<12>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        default: e = launch_fwd_static<16>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+    }
+    if (e != cudaSuccess) return check_cuda(e, "cui_born_forward_static");
+    // every (group, slot, object, element) partial is written by the contraction, so nothing needs clearing
+    const int64_t n = static_cast<int64_t>(p->S) * n_objects * p->E;
+    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(part, groups, n, G);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "cui_born_forward_static reduce");
+    MixArgs m;
+    m.G = G; m.row_slot = p->row_slot; m.row_mix = p->row_mix; m.row_fl = p->row_fl;
+    m.mix_nact = p->mix_nact; m.mix_nf = p->mix_nf; m.mix_pref_off = p->mix_pref_off; m.mix_act_off = p->mix_act_off;
+    m.act = p->act; m.pref = p->pref; m.n_obs = p->n_obs; m.B = n_objects; m.E = p->E;
+    m.u = reinterpret_cast<float2*>(u); m.ldu = ld_u;
+    const int64_t blocks = (p->n_obs * n_objects * 32 + 255) / 256;
+    mix_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(m);
+    count_launch();
+    return check_cuda(cudaGetLastError(), "cui_born_forward_static mix");
+}

@@ -185,6 +185,20 @@ cui_status cui_born_size(const cui_born_plan* plan, int64_t* n_observations, int
 cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
                             int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream);
 
+/* Forward that allocates nothing.  No counterpart in the reference: its MEX
+ * allocates device memory on every call.  Same operation and arguments as
+ * cui_born_forward, for callers that must not allocate device memory when
+ * they apply the operator (a stream being captured into a CUDA graph, plug-in
+ * hosts with a fixed device-memory budget, real-time loops).  Partial sums
+ * live in a 16 MiB file-scope device array that each GPU loading the library
+ * holds until exit, so slots x n_objects x elements x 16 B must not exceed
+ * 16 MiB (else CUI_ERR_INVALID_ARG).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (other streams, other plans, other threads) race. */
+cui_status cui_born_forward_static(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
+                                   int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream);
+
 /* Adjoint, mode 2 (.cu:914-921; operator_born.m:480-596):
  *   gamma_hat[:, b] = Phi^H * u[:, b]. */
 cui_status cui_born_adjoint(cui_born_plan* plan, const cui_complex32* u, int64_t ld_u,
