@@ -118,6 +118,8 @@ _SIGNATURES = {
                                          C.c_int64]),
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
+    "cui_born_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "cui_born_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "cui_born_timing_read": (C.c_int, [C.c_void_p, C.POINTER(BornTiming)]),
     "cui_status_string": (C.c_char_p, [C.c_int]),
@@ -344,6 +346,17 @@ class OperatorBorn:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_precision(self, precision: str) -> None:
+        """``"fp32"`` (CUDA cores) or ``"bf16x3"`` (split-BF16 tcgen05 tensor cores)."""
+        _check(self._lib.cui_born_set_precision(self._plan, {"fp32": 0, "bf16x3": 1}[precision]))
+        self.precision = precision
+
+    def device_status(self) -> int:
+        """Read and clear the device status word (raises CuiError on a timed-out wait)."""
+        s = C.c_int32()
+        _check(self._lib.cui_born_plan_status(self._plan, C.byref(s)))
+        return s.value
 
     def timing(self, enable: Optional[bool] = None) -> dict:
         """Enable/disable per-kernel event timing, or read (and clear) the sums."""

@@ -108,6 +108,16 @@ struct Plan {
     std::vector<int> h_f_slot_ptr, h_f_slot_list, h_slot_f;
     HostMeta h_meta;                 // emptied once uploaded
 
+    // split-BF16 tensor-core path (cui_tc.cu): 0 = FP32 CUDA cores, 1 = BF16x3 tensor cores
+    int precision = 0;
+    uint32_t* tb = nullptr;          // band arrays [4][F][Nz][Noy][ppx][Nb] of packed bf16x2
+    int64_t tb_vstride = 0;
+    int Nb = 0;                      // band entries per residue
+    int Epad = 0;                    // elements rounded up to a multiple of 8
+    int Jpad = 0;                    // points per residue rounded up to a multiple of 8
+    size_t tc_bytes = 0;
+    int* ws_status = nullptr;        // device status word (bounded waits that gave up)
+
     // per-kernel timing (diagnostics): event pairs around contraction launches
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -144,6 +154,12 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
 size_t fwd_smem_bytes(const Plan* p, int nc);
 size_t adj_smem_bytes(const Plan* p, int nc);
 bool launch_shapes_ok(const Plan* p, std::string* why);
+// tensor-core path
+bool tc_supported(const Plan* p, std::string* why);
+cui_status tc_prepare(Plan& p);
+cudaError_t launch_adj_tc(Plan* p, int B, cudaStream_t st);
+cudaError_t launch_fwd_tc(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st);
+
 // timing hooks around a contraction launch (no-ops unless timing is enabled)
 cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st);
 cudaError_t timing_end(Plan* p, cudaStream_t st);

@@ -583,7 +583,9 @@ int grid_1d(int64_t n, int threads) {
 
 cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
     cudaError_t e;
-    switch (pick_nc(p->max_slots_per_f)) {
+    if (p->precision == 1) {
+        e = launch_fwd_tc(p, gamma, ldg, B, st);
+    } else switch (pick_nc(p->max_slots_per_f)) {
         case 1: e = launch_fwd<1>(p, gamma, ldg, B, st); break;
         case 2: e = launch_fwd<2>(p, gamma, ldg, B, st); break;
         case 4: e = launch_fwd<4>(p, gamma, ldg, B, st); break;
@@ -617,6 +619,13 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (p->precision == 1) {
+        if ((e = launch_adj_tc(p, B, st)) != cudaSuccess) return e;
+        const int64_t m = static_cast<int64_t>(B) * p->P;
+        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, p->adj_nfc, B, p->P, g, ldg);
+        count_launch();
+        return cudaGetLastError();
+    }
     switch (pick_nc(p->max_slots_per_f)) {
         case 1: e = launch_adj<1>(p, B, st); break;
         case 2: e = launch_adj<2>(p, B, st); break;

@@ -225,6 +225,16 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
                              const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects,
                              cui_complex64* grad, int64_t ld_grad, double* loss);
 
+/* ---- precision ------------------------------------------------------------
+ * CUI_PRECISION_FP32: FP32 CUDA-core contractions (default).
+ * CUI_PRECISION_BF16X3: the adjoint contraction runs on the tcgen05 tensor
+ * cores with every operand split into bf16 hi + lo and the three products
+ * hi*hi + hi*lo + lo*hi accumulated in FP32 (2D setups, <= 128 elements).
+ * Switching to BF16X3 builds the split band tables once (allocates). */
+typedef enum { CUI_PRECISION_FP32 = 0, CUI_PRECISION_BF16X3 = 1 } cui_precision;
+
+cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precision);
+
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Device time of the two contraction kernels, from CUDA events recorded on
  * the launching stream around each launch while timing is enabled. */
@@ -236,6 +246,9 @@ typedef struct {
 } cui_born_timing;
 
 cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable);
+/* Reads and clears the plan's device status word; CUI_ERR_TIMEOUT when a
+ * bounded device-side wait gave up since the last call. */
+cui_status cui_born_plan_status(cui_born_plan* plan, int32_t* device_status);
 /* Waits for the recorded events, returns the sums and clears them. */
 cui_status cui_born_timing_read(cui_born_plan* plan, cui_born_timing* out);
 

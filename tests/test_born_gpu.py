@@ -273,3 +273,39 @@ def test_plain_c_harness():
     assert out.returncode == 0, out.stdout + out.stderr
     res = json.loads(out.stdout.strip().splitlines()[-1])
     assert res["ok"] and res["dot_product_rel_err"] < 1e-6
+
+
+@pytest.mark.parametrize("name", ["c0", "c1", "c2", "ragged"])
+def test_bf16x3_tensor_core_matches_oracle(name):
+    """Split-BF16 tcgen05 forward and adjoint: relative L2 <= 1e-5 against the FP64 oracle."""
+    b = built(name)
+    B = b.cfg.n_objects
+    op = make_operator(b, "lateral", max_objects=B)
+    op.set_precision("bf16x3")
+    gamma = configs.make_gamma(b.cfg, complex_values=True)
+    u = op.forward(dev(gamma)).cpu().numpy()
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
+    y = rand_obs(b, B, 7)
+    g = op.adjoint(dev(y)).cpu().numpy()
+    assert rel_l2(g, adjoint_quick_cpu(b.op, y)) <= TOL
+    assert op.device_status() == 0
+
+
+def test_bf16x3_vjp_matches_oracle():
+    b = built("c1")
+    op = make_operator(b, "lateral", max_objects=1)
+    op.set_precision("bf16x3")
+    gamma_true = configs.make_gamma(b.cfg)
+    u_meas = configs.add_noise(forward_quick_cpu(b.op, gamma_true), 30.0, seed=5)
+    gamma = np.random.default_rng(21).standard_normal(gamma_true.shape)
+    r = forward_quick_cpu(b.op, gamma) - u_meas
+    grad, loss = op.vjp(dev(gamma), dev(u_meas))
+    assert rel_l2(grad.cpu().numpy(), adjoint_quick_cpu(b.op, r)) <= TOL
+
+
+def test_bf16x3_refused_for_3d():
+    from comp_ui_toolbox_gb300 import CuiError
+    op = make_operator(built("c3"), "lateral", max_objects=1)
+    with pytest.raises(CuiError) as ei:
+        op.set_precision("bf16x3")
+    assert ei.value.status == 2
