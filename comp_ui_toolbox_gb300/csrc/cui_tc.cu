@@ -101,47 +101,55 @@ __device__ __forceinline__ void fetch_band(uint32_t (&be)[kMaxBandPerThread], co
         const int idx = tid + kTcThreads * m;
         uint32_t w = 0u;
         if (idx < n) {
-            const int v = idx / (NCH + 3), i = idx - v * (NCH + 3);
+            const int v = idx >= NCH + 3 ? 1 : 0, i = idx - v * (NCH + 3);
             if (i < Nb) w = __ldg(band + static_cast<int64_t>(v) * vstride + i);
         }
         be[m] = w;
     }
 }
 
-// chunk ch of variant v holds band entries ch..ch+3 (16 B at sA + (v*NCH + ch)*16)
+// chunk ch of variant v holds band entries ch..ch+3 (16 B at sA + (v*NCH + ch)*16).
+// A warp's 32 entries are written in 4 rounds; in round q lane l stores word
+// l%4 of entry 8q + l/4 (taken from that lane by a shuffle), which puts the 32
+// stores of a round into 32 distinct banks.
 __device__ __forceinline__ void store_chunks(unsigned char* sA, const uint32_t (&be)[kMaxBandPerThread], int NCH, int tid) {
     const int n = 2 * (NCH + 3);
+    const int lane = tid & 31, wbase = tid - lane;
 #pragma unroll
     for (int m = 0; m < kMaxBandPerThread; ++m) {
-        const int idx = tid + kTcThreads * m;
-        if (idx < n) {
-            const int v = idx / (NCH + 3), i = idx - v * (NCH + 3);
+        if (wbase + kTcThreads * m >= n) break;  // uniform over the warp
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
+        for (int q = 0; q < 4; ++q) {
+            const int src = 8 * q + (lane >> 2), t = lane & 3;
+            const uint32_t w = __shfl_sync(0xffffffffu, be[m], src);
+            const int idx = wbase + kTcThreads * m + src;
+            if (idx < n) {
+                const int v = idx >= NCH + 3 ? 1 : 0, i = idx - v * (NCH + 3);
                 const int ch = i - t;
-                if (ch >= 0 && ch < NCH)
-                    *reinterpret_cast<uint32_t*>(sA + (static_cast<size_t>(v) * NCH + ch) * 16 + 4 * t) = be[m];
+                if (ch >= 0 && ch < NCH) *reinterpret_cast<uint32_t*>(sA + (static_cast<size_t>(v) * NCH + ch) * 16 + 4 * t) = w;
             }
         }
     }
 }
 
-// byte offset of B entry (row n, K index kk) in the canonical K-major layout
-__device__ __forceinline__ int b_offset(int n, int kk, int SBO) {
-    return (n >> 3) * SBO + (kk >> 3) * 128 + (n & 7) * 16 + (kk & 7) * 2;
+// byte offset of the first stacked B row of column c at K index kk; the rows of
+// B2 hi, B1 lo, B2 lo follow at +2, +4, +6 SBO (16 rows = two 8-row groups)
+__device__ __forceinline__ int b_base(int c, int kk, int SBO) {
+    return (c >> 3) * SBO + (kk >> 3) * 128 + (c & 7) * 16 + (kk & 7) * 2;
 }
 
-// writes the four stacked B entries of column c, K position kk: rows c (B1 hi),
-// 16+c (B2 hi), 32+c (B1 lo), 48+c (B2 lo)
-__device__ __forceinline__ void store_b(unsigned char* sB, int c, int kk, int SBO, float b1x, float b1y, float b2x,
-                                        float b2y) {
-    uint32_t h1, l1, h2, l2;
-    split2(b1x, b1y, h1, l1);
-    split2(b2x, b2y, h2, l2);
-    *reinterpret_cast<uint32_t*>(sB + b_offset(c, kk, SBO)) = h1;
-    *reinterpret_cast<uint32_t*>(sB + b_offset(kCols16 + c, kk, SBO)) = h2;
-    *reinterpret_cast<uint32_t*>(sB + b_offset(2 * kCols16 + c, kk, SBO)) = l1;
-    *reinterpret_cast<uint32_t*>(sB + b_offset(3 * kCols16 + c, kk, SBO)) = l2;
+// Stores B1 = (x, y) and B2 = (-y, x) (hi and lo) at byte offset off:
+// B2's bf16 words are B1's with the halves swapped and the new low half negated,
+// because rounding to bf16 commutes with negation.
+__device__ __forceinline__ void store_b_rot(unsigned char* sB, int off, int SBO, float x, float y) {
+    uint32_t h1, l1;
+    split2(x, y, h1, l1);
+    const uint32_t h2 = __byte_perm(h1, 0, 0x1032) ^ 0x00008000u;
+    const uint32_t l2 = __byte_perm(l1, 0, 0x1032) ^ 0x00008000u;
+    *reinterpret_cast<uint32_t*>(sB + off) = h1;
+    *reinterpret_cast<uint32_t*>(sB + off + 2 * SBO) = h2;
+    *reinterpret_cast<uint32_t*>(sB + off + 4 * SBO) = l1;
+    *reinterpret_cast<uint32_t*>(sB + off + 6 * SBO) = l2;
 }
 
 // Per K step: D1 (+)= A_hi x B[0:64) and D2 (+)= A_lo x B[0:32).  A K step
@@ -162,24 +170,23 @@ __device__ __forceinline__ void issue_unit(uint32_t t_d1, uint32_t t_d2, uint32_
     }
 }
 
-// adds 16 consecutive TMEM columns of the calling thread's lane into dst
-__device__ __forceinline__ void tmem_add16(uint32_t taddr, float (&dst)[kCols16]) {
-    float t[16];
-    tc::tmem_ld16(taddr, t);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int u = 0; u < 16; ++u) dst[u] += t[u];
-}
-
-// adds the unit's result (re/im of the 16 columns) for the calling thread's lane
+// adds the unit's result (re/im of the 16 columns) for the calling thread's lane:
+// re = A_hi B1_hi + A_hi B1_lo + A_lo B1_hi, im likewise with B2 (two TMEM waits)
 __device__ __forceinline__ void add_unit(uint32_t t_d1, uint32_t t_d2, uint32_t lane_base, float (&re)[kCols16],
                                          float (&im)[kCols16]) {
-    tmem_add16(t_d1 + lane_base, re);       // A_hi B1_hi
-    tmem_add16(t_d1 + lane_base + 32, re);  // A_hi B1_lo
-    tmem_add16(t_d2 + lane_base, re);       // A_lo B1_hi
-    tmem_add16(t_d1 + lane_base + 16, im);  // A_hi B2_hi
-    tmem_add16(t_d1 + lane_base + 48, im);  // A_hi B2_lo
-    tmem_add16(t_d2 + lane_base + 16, im);  // A_lo B2_hi
+    float a[16], b[16], c[16];
+    tc::tmem_ld16(t_d1 + lane_base, a);
+    tc::tmem_ld16(t_d1 + lane_base + 32, b);
+    tc::tmem_ld16(t_d2 + lane_base, c);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) re[u] += (a[u] + b[u]) + c[u];
+    tc::tmem_ld16(t_d1 + lane_base + 16, a);
+    tc::tmem_ld16(t_d1 + lane_base + 48, b);
+    tc::tmem_ld16(t_d2 + lane_base + 16, c);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) im[u] += (a[u] + b[u]) + c[u];
 }
 
 // ---------------------------------------------------------------------------
@@ -203,7 +210,7 @@ struct AdjTcArgs {
 //   [0, SBB)             stacked B (SBB = 64 rows x 2*Epad bf16 = 256*Epad)
 //   [SBB, +2*NCH*16)     spread chunks of A hi, A lo (NCH = 128 + Epad)
 //   then sG [Nx] float2, then bar (8 B), tslot (4 B), slots [16] int
-__global__ void __launch_bounds__(kTcThreads, 4) adj_tc_kernel(const AdjTcArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 3) adj_tc_kernel(const AdjTcArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int SBB = 256 * a.Epad;
     const int NCH = 128 + a.Epad;
@@ -258,12 +265,14 @@ __global__ void __launch_bounds__(kTcThreads, 4) adj_tc_kernel(const AdjTcArgs a
             if (tid < kCols16) sSlot[tid] = (tid < nc) ? a.f_slot_list[s0 + c0 + tid] : 0;
             __syncthreads();
             // ---- B: V columns, element order reversed, complex interleaved along K ----
+            // lanes -> (column mod 8, element mod 4): the 32 stores of a warp hit 32 banks
             for (int idx = tid; idx < kCols16 * a.Epad; idx += kTcThreads) {
-                const int c = idx / a.Epad, ep = idx - c * a.Epad;
+                const int t = idx & 31, w = idx >> 5;
+                const int c = ((t >> 2) & 7) + 8 * (w & 1), ep = 4 * (w >> 1) + (t & 3);
                 const int e = a.Ex - 1 - ep;
                 float2 v = make_float2(0.f, 0.f);
                 if (c < nc && e >= 0) v = __ldg(a.V + (static_cast<int64_t>(sSlot[c]) * a.B + b) * a.E + e);
-                store_b(sB, c, 2 * ep, SBO, v.x, v.y, v.y, -v.x);
+                store_b_rot(sB, b_base(c, 2 * ep, SBO), SBO, v.x, v.y);  // imaginary part comes out negated
             }
         }
         store_chunks(sA, be, NCH, tid);
@@ -285,7 +294,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) adj_tc_kernel(const AdjTcArgs a
         advance(fn, cn, rn);
         while (fn < f_hi && a.f_slot_ptr[fn + 1] == a.f_slot_ptr[fn]) ++fn;
         if (fn < f_hi) fetch_band(be, band_of(fn, rn), a.vstride, a.Nb, NCH, tid);
-        const bool ok = tc::bar_wait(bar, phase);
+        const bool ok = (tid == 0) ? tc::bar_wait(bar, phase) : true;  // one poller; the rest park at the barrier
         phase ^= 1u;
         if (__syncthreads_or(!ok)) {
             failed = true;
@@ -299,10 +308,10 @@ __global__ void __launch_bounds__(kTcThreads, 4) adj_tc_kernel(const AdjTcArgs a
         add_unit(t_d1, t_d2, lane_base, zr, zi);
         float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int c = 0; c < kCols16; ++c) {
+        for (int c = 0; c < kCols16; ++c) {  // Z = zr - i*zi
             const float2 p = pq[c];
-            acc.x = fmaf(p.x, zr[c], fmaf(p.y, zi[c], acc.x));
-            acc.y = fmaf(p.x, zi[c], fmaf(-p.y, zr[c], acc.y));
+            acc.x = fmaf(p.x, zr[c], fmaf(-p.y, zi[c], acc.x));
+            acc.y = fmaf(-p.x, zi[c], fmaf(-p.y, zr[c], acc.y));
         }
         if (tid < Nj_r) {
             float2 g = sG[x];
@@ -346,17 +355,20 @@ struct FwdTcArgs {
     int* status;
 };
 
-// dynamic shared memory (bytes): stacked B (256*Jpad), A chunks hi/lo (2 x NCH x 16,
-// NCH = 128 + Jpad), bar, tslot, slots[16]
-__global__ void __launch_bounds__(kTcThreads, 3) fwd_tc_kernel(const FwdTcArgs a) {
+// Two-stage pipeline: shared-memory stages and TMEM accumulators alternate, so
+// the MMAs of unit u+1 run while unit u is read out and unit u+2 is staged.
+// dynamic shared memory (bytes): 2 stages x [stacked B (256*Jpad), A chunks hi/lo
+// (2 x NCH x 16, NCH = 128 + Jpad)], 2 mbarriers, tslot, slots[16]
+constexpr uint32_t kFwdTmemCols = 256;  // 2 stages x (D1 64 + D2 32), stage stride 128 columns
+
+__global__ void __launch_bounds__(kTcThreads, 2) fwd_tc_kernel(const FwdTcArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int SBB = 256 * a.Jpad;
     const int NCH = 128 + a.Jpad;
-    unsigned char* sB = smem;
-    unsigned char* sA = smem + SBB;
-    unsigned char* tail = sA + 2 * NCH * 16;
-    uint64_t* barp = reinterpret_cast<uint64_t*>(tail);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(barp + 1);
+    const int STAGE = SBB + 2 * NCH * 16;
+    unsigned char* tail = smem + 2 * STAGE;
+    uint64_t* barp = reinterpret_cast<uint64_t*>(tail);  // [2]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(barp + 2);
     int* sSlot = reinterpret_cast<int*>(tslot + 1);
 
     const int grp = blockIdx.x, f = blockIdx.y;
@@ -368,23 +380,27 @@ __global__ void __launch_bounds__(kTcThreads, 3) fwd_tc_kernel(const FwdTcArgs a
     const int nc = min(kCols16, ns - c0);
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid < kCols16) sSlot[tid] = (tid < nc) ? a.f_slot_list[s0 + c0 + tid] : 0;
-    const uint32_t bar = tc::smem_u32(barp);
     const int SBO = 32 * a.Jpad;
-    if (tid == 0) tc::bar_init(bar, 1);
-    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), kTmemCols);
+    if (tid == 0) {
+        tc::bar_init(tc::smem_u32(barp), 1);
+        tc::bar_init(tc::smem_u32(barp + 1), 1);
+    }
+    if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), kFwdTmemCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t t_d1 = tmem, t_d2 = tmem + 64;
     const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
-    uint32_t phase = 0;
+    uint32_t phase0 = 0, phase1 = 0;
     bool failed = false;
     const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg;
 
-    // each thread owns one point j of every unit and the columns c = ct0 + cstride*m
+    // each thread owns one point j of every unit and the columns c = ct0 + cstride*((m + g) mod ncol);
+    // the rotation by the lane group g spreads a warp's B stores over all banks
     const int jt = tid % a.Jpad, ct0 = tid / a.Jpad, cstride = kTcThreads / a.Jpad;
-    const int ncol = (kCols16 + cstride - 1) / cstride;  // columns per thread (<= 16)
+    const int ncol = (kCols16 + cstride - 1) / cstride;  // columns per thread (<= 16), a power of two
+    const int g = (tid >> 2) & 7;
+    auto col = [&](int m) { return ct0 + cstride * ((m + g) & (ncol - 1)); };
     float accr[kCols16], acci[kCols16];
 #pragma unroll
     for (int c = 0; c < kCols16; ++c) accr[c] = acci[c] = 0.f;
@@ -394,52 +410,70 @@ __global__ void __launch_bounds__(kTcThreads, 3) fwd_tc_kernel(const FwdTcArgs a
     uint32_t be[kMaxBandPerThread];
     float2 pq[kCols16];
     float2 gq = make_float2(0.f, 0.f);
+    auto nj_of = [&](int u) {
+        const int r = u % a.ppx;
+        return (r < a.Nx) ? (a.Nx - r + a.ppx - 1) / a.ppx : 0;
+    };
     auto fetch = [&](int u) {
         const int z = line0 + u / a.ppx, r = u % a.ppx;
-        const int Nj_r = (r < a.Nx) ? (a.Nx - r + a.ppx - 1) / a.ppx : 0;
+        const int Nj_r = nj_of(u);
         const int64_t pt = static_cast<int64_t>(z) * a.Nx + r + static_cast<int64_t>(a.ppx) * jt;
         fetch_band(be, a.tb + ((static_cast<int64_t>(f) * a.Nz + z) * a.ppx + r) * a.Nb, a.vstride, a.Nb, NCH, tid);
         gq = (jt < Nj_r) ? __ldg(gam + pt) : make_float2(0.f, 0.f);
 #pragma unroll
         for (int m = 0; m < kCols16; ++m) {
-            const int c = ct0 + cstride * m;
+            const int c = col(m);
             pq[m] = (m < ncol && c < nc && jt < Nj_r) ? __ldg(a.p_in + static_cast<int64_t>(sSlot[c]) * a.P + pt)
                                                       : make_float2(0.f, 0.f);
         }
     };
-    if (U > 0) fetch(0);
-    for (int u = 0; u < U && !failed; ++u) {
-        const int r = u % a.ppx;
-        const int Nj_r = (r < a.Nx) ? (a.Nx - r + a.ppx - 1) / a.ppx : 0;
-        const int ks = (Nj_r + 7) / 8;
-        store_chunks(sA, be, NCH, tid);
+    auto store = [&](int st) {
+        unsigned char* sB = smem + st * STAGE;
+        store_chunks(sB + SBB, be, NCH, tid);
 #pragma unroll
         for (int m = 0; m < kCols16; ++m) {
-            const int c = ct0 + cstride * m;
+            const int c = col(m);
             if (m < ncol && c < kCols16) {
                 const float2 p = pq[m];
                 const float qx = p.x * gq.x - p.y * gq.y, qy = p.x * gq.y + p.y * gq.x;
-                store_b(sB, c, 2 * jt, SBO, qx, -qy, qy, qx);
+                store_b_rot(sB, b_base(c, 2 * jt, SBO), SBO, qx, -qy);
             }
         }
+    };
+    auto issue = [&](int u, int st) {  // thread 0
+        tc::fence_after_sync();
+        const uint32_t base = tc::smem_u32(smem + st * STAGE);
+        const uint32_t td = tmem + 128u * st;
+        issue_unit(td, td + 64, base + SBB, NCH, base, SBO, (nj_of(u) + 7) / 8);
+        tc::commit(tc::smem_u32(barp + st));
+    };
+
+    if (U > 0) {
+        fetch(0);
+        store(0);
         tc::fence_async_smem();
         __syncthreads();
+        if (tid == 0) issue(0, 0);
+        if (U > 1) fetch(1);
+    }
+    for (int u = 0; u < U; ++u) {
+        const int st = u & 1;
+        if (u + 1 < U) store(st ^ 1);  // overlaps MMA(u); stage st^1 was released when MMA(u-1) completed
+        tc::fence_async_smem();
+        bool ok = true;
         if (tid == 0) {
-            tc::fence_after_sync();
-            issue_unit(t_d1, t_d2, tc::smem_u32(sA), NCH, tc::smem_u32(sB), SBO, ks);
-            tc::commit(bar);
+            ok = tc::bar_wait(tc::smem_u32(barp + st), st ? phase1 : phase0);
         }
-        if (u + 1 < U) fetch(u + 1);  // in flight while the MMAs run
-        const bool ok = tc::bar_wait(bar, phase);
-        phase ^= 1u;
+        if (st) phase1 ^= 1u; else phase0 ^= 1u;
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
+        if (tid == 0 && u + 1 < U) issue(u + 1, st ^ 1);
+        if (u + 2 < U) fetch(u + 2);
         tc::fence_after_sync();
-        add_unit(t_d1, t_d2, lane_base, accr, acci);
+        add_unit(tmem + 128u * st, tmem + 128u * st + 64, lane_base, accr, acci);
         tc::fence_before_sync();
-        __syncthreads();
     }
     if (failed && tid == 0) atomicOr(a.status, 1);
     // ---- epilogue: lanes = elements e' ----
@@ -450,14 +484,13 @@ __global__ void __launch_bounds__(kTcThreads, 3) fwd_tc_kernel(const FwdTcArgs a
             if (c < nc)
                 a.part[((static_cast<int64_t>(grp) * a.S + sSlot[c]) * a.B + b) * a.E + e] = make_float2(accr[c], acci[c]);
     }
-    tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::tmem_dealloc(tmem, kFwdTmemCols);
 }
 
 size_t fwd_tc_smem(const Plan* p) {
     const size_t Jpad = static_cast<size_t>(p->Jpad);
-    return 256 * Jpad + 2 * (128 + Jpad) * 16 + 8 + 8 + 4 * kCols16 + 64;
+    return 2 * (256 * Jpad + 2 * (128 + Jpad) * 16) + 16 + 8 + 4 * kCols16 + 64;
 }
 
 size_t adj_tc_smem(const Plan* p) {
