@@ -57,11 +57,70 @@ def dist_env():
 
 
 def peaks():
+    """Roofline denominators: the machine's measured copy bandwidth and cuBLAS bf16 rate, else the fallback."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), float(d.get("sm_max_mhz", 2070.0)), "measured"
-    return 6800.0, 2070.0, "fallback"
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0)), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def launch_traffic(workload: str, kernel: str, n_freq: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (scaled by frequencies), or None."""
+    tf = ROOT / "profiles" / "traffic.json"
+    if not tf.exists():
+        return None
+    rec = json.loads(tf.read_text()).get(f"{workload}:{kernel}")
+    if not rec:
+        return None
+    return rec["bytes_per_frequency"] * n_freq
+
+
+def roofline_of(args, info, kt, B, clk):
+    """Roofline of the dominant contraction kernel of one apply.
+
+    Split-BF16 (tensor cores): algorithmic work = 24 FLOP per complex MAC
+    (4 real products x 3 bf16 products x 2) over the S*P*E complex MACs of a
+    dense apply, padding excluded, against the measured bf16 tensor peak.
+    FP32 (CUDA cores): 8 FLOP per complex MAC against 152 SMs x 128 lanes x 2 x
+    the sampled SM clock.  Both carry the HBM view (compulsory bytes: incident
+    fields, transfer-function table, gamma and the output, once per launch).
+    """
+    pk = peaks()
+    macs = info["contraction_macs"] * B
+    dom = "forward" if kt["ms_forward"] >= kt["ms_adjoint"] else "adjoint"
+    t_launch = kt["ms_" + dom] / max(1, kt["n_" + dom]) / 1e3
+    P = info["n_points"]
+    compulsory = info["table_bytes"] + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
+    tc = args.precision != "fp32"
+    kernel = {("forward", True): "fwd_tc_kernel", ("adjoint", True): "adj_tc_kernel",
+              ("forward", False): "fwd_dense_kernel", ("adjoint", False): "adj_dense_kernel"}[(dom, tc)]
+    traffic = launch_traffic(args.workload, kernel, args.n_freq_used)
+    hbm = {"compulsory_bytes": compulsory, "achieved_gbs": compulsory / t_launch / 1e9,
+           "peak_gbs": pk["hbm_gbs"], "frac": compulsory / t_launch / 1e9 / pk["hbm_gbs"],
+           "traffic_over_compulsory": (traffic / compulsory) if traffic else None}
+    sm_mhz = clk.get("sm_mhz") or pk["sm_max_mhz"]
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    launch_ms = {"forward": kt["ms_forward"] / max(1, kt["n_forward"]),
+                 "adjoint": kt["ms_adjoint"] / max(1, kt["n_adjoint"])}
+    if tc:
+        flops = 24.0 * macs
+        achieved = flops / t_launch / 1e12
+        return {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": traffic, "kernel": kernel,
+                "peak_source": f"{pk['source']} bf16 burst (MEASURED_PEAKS.json bf16_tflops)"
+                               if pk["source"] == "measured" else "fallback",
+                "achieved_definition": "24 FLOP per complex MAC (4 real x 3 split-BF16 products x 2) x S*P*E "
+                                       "complex MACs per launch (padding excluded) / average launch time",
+                "flops_per_launch": flops, "hbm": hbm, "launch_ms": launch_ms}
+    flops = 8.0 * macs
+    achieved = flops / t_launch / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak, "traffic": traffic, "kernel": kernel,
+            "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median sampled SM clock",
+            "achieved_definition": "8 FLOP per complex MAC x S*P*E complex MACs per launch / average launch time",
+            "flops_per_launch": flops, "hbm": hbm, "launch_ms": launch_ms}
 
 
 class ClockSampler:
@@ -182,6 +241,7 @@ def run_ours(args):
     w = workload(args.workload)
     if args.n_freq:
         w.f = w.f[: args.n_freq]
+    args.n_freq_used = len(w.f)
     B = w.n_objects if args.workload == "2d-batched" else 1
     t0 = time.perf_counter()
     op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=B)
@@ -257,40 +317,14 @@ def run_ours(args):
            "path": "cui_born_vjp_host: FP64 host buffers -> FP32 pinned staging -> H2D -> VJP -> D2H -> FP64"}
 
     # roofline of the dominant contraction kernel
-    hbm, sm_max, peak_kind = peaks()
-    info = op.info
-    macs = info["contraction_macs"] * B  # complex MACs of one dense apply
-    dom = "forward" if kt["ms_forward"] >= kt["ms_adjoint"] else "adjoint"
-    n_l = kt["n_" + dom] or 1
-    t_launch = kt["ms_" + dom] / n_l / 1e3
-    phi_bytes = 8.0 * macs                                    # Phi-equivalent bytes (reference formulation)
-    compulsory = info["table_bytes"] + info["incident_bytes"] + 8 * B * (P if dom == "forward" else P)
-    flops = 8.0 * macs
-    sm_mhz = None
     clk = clocks.summary()
-    sm_mhz = clk.get("sm_mhz") or sm_max
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12             # TFLOP/s of the CUDA cores at the sampled clock
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        tj = json.loads(tf.read_text())
-        traffic = tj.get(f"{args.workload}:{dom}")
-    roofline = {"bound": "hbm", "achieved": phi_bytes / t_launch / 1e9, "peak": hbm, "unit": "GB/s",
-                "frac": phi_bytes / t_launch / 1e9 / hbm, "traffic": traffic,
-                "kernel": f"{dom} contraction ({'fwd_dense_kernel' if dom == 'forward' else 'adj_dense_kernel'})",
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "achieved_definition": "Phi-equivalent bytes (8 B per complex MAC, the reference's materialised "
-                                       "Phi read once) / average launch time",
-                "compulsory_bytes": compulsory, "compulsory_frac": compulsory / t_launch / 1e9 / hbm,
-                "fp32": {"achieved_tflops": flops / t_launch / 1e12, "peak_tflops": fp32_peak,
-                         "frac": flops / t_launch / 1e12 / fp32_peak,
-                         "peak_definition": "152 SMs x 128 FP32 lanes x 2 flops x median sampled SM clock"},
-                "launch_ms": {"forward": kt["ms_forward"] / max(1, kt["n_forward"]),
-                              "adjoint": kt["ms_adjoint"] / max(1, kt["n_adjoint"])}}
+    roofline = roofline_of(args, op.info, kt, B, clk)
+    info = op.info
+    macs = info["contraction_macs"] * B
 
     line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f32 (adjoint: bf16x3 split, f32 accumulate)",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16x3 (split-BF16 operands, f32 accumulate)",
             "data": "synthetic (seeded)", "config": workload_config(w, B),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "clocks": clk,
             "plan": {"build_s": t_build, "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
