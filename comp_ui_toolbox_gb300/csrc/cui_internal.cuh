@@ -116,6 +116,15 @@ struct Plan {
     int Epad = 0;                    // elements rounded up to a multiple of 8
     int Jpad = 0;                    // points per residue rounded up to a multiple of 8
     size_t tc_bytes = 0;
+    // line-unit tensor-core kernels (cui_tc2.cu; 2D, 4 grid points per pitch):
+    // raw band rows [2][F][Nz][RowW] of packed bf16x2 (re, im), hi then lo
+    int tc2 = 0;                     // 1 when the plan runs the line-unit kernels
+    uint32_t* tr = nullptr;
+    int64_t tr_vstride = 0;          // entries per variant
+    int RowW = 0;                    // entries per row (lateral offsets rounded up to 4, zero padded)
+    float2* p_rm = nullptr;          // incident fields residue-major [S][Nz][4][Jp] (adjoint epilogue)
+    int Jp = 0;                      // points per residue class, rounded up to even
+    float2* ws_galign = nullptr;     // [max_objects][P] aligned copy of a misaligned gamma (forward)
     int* ws_status = nullptr;        // device status word (bounded waits that gave up)
 
     // per-kernel timing (diagnostics): event pairs around contraction launches
@@ -159,6 +168,12 @@ bool tc_supported(const Plan* p, std::string* why);
 cui_status tc_prepare(Plan& p);
 cudaError_t launch_adj_tc(Plan* p, int B, cudaStream_t st);
 cudaError_t launch_fwd_tc(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st);
+// line-unit tensor-core kernels: launch the contraction and report how many
+// partial-sum slabs (line groups / frequency chunks) the reduction must add
+bool tc2_supported(const Plan* p, std::string* why);
+cui_status tc2_prepare(Plan& p);
+cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* groups);
+cudaError_t launch_adj_tc2(Plan* p, int B, cudaStream_t st, int* nfc);
 
 // timing hooks around a contraction launch (no-ops unless timing is enabled)
 cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st);

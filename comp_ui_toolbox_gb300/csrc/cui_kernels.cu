@@ -583,7 +583,10 @@ int grid_1d(int64_t n, int threads) {
 
 cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
     cudaError_t e;
-    if (p->precision == 1) {
+    int groups = p->fwd_groups;
+    if (p->precision == 1 && p->tc2) {
+        e = launch_fwd_tc2(p, gamma, ldg, B, st, &groups);
+    } else if (p->precision == 1) {
         e = launch_fwd_tc(p, gamma, ldg, B, st);
     } else switch (pick_nc(p->max_slots_per_f)) {
         case 1: e = launch_fwd<1>(p, gamma, ldg, B, st); break;
@@ -595,7 +598,7 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     }
     if (e != cudaSuccess) return e;
     const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
-    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, p->fwd_groups, n, p->ws_G);
+    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     MixArgs m;
@@ -620,9 +623,14 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (p->precision == 1) {
-        if ((e = launch_adj_tc(p, B, st)) != cudaSuccess) return e;
+        int nfc = p->adj_nfc;
+        if (p->tc2) {
+            if ((e = launch_adj_tc2(p, B, st, &nfc)) != cudaSuccess) return e;
+        } else if ((e = launch_adj_tc(p, B, st)) != cudaSuccess) {
+            return e;
+        }
         const int64_t m = static_cast<int64_t>(B) * p->P;
-        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, p->adj_nfc, B, p->P, g, ldg);
+        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg);
         count_launch();
         return cudaGetLastError();
     }

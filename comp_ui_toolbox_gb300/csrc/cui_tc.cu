@@ -592,7 +592,15 @@ extern "C" cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precis
     if (precision != CUI_PRECISION_BF16X3) return set_error(CUI_ERR_INVALID_ARG, "unknown precision");
     cudaError_t e = cudaSetDevice(plan->p.device);
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
-    cui_status s = tc_prepare(plan->p);
+    Plan& p = plan->p;
+    if (!p.ws_status) {
+        cui_status s = device_alloc(p, reinterpret_cast<void**>(&p.ws_status), sizeof(int));
+        if (s != CUI_OK) return s;
+        if ((e = cudaMemset(p.ws_status, 0, sizeof(int))) != cudaSuccess) return check_cuda(e, "cudaMemset");
+    }
+    std::string why;
+    // line-unit kernels where the geometry allows them, else the residue-unit kernels
+    cui_status s = (!p.tc2 && !p.tb && tc2_supported(&p, &why)) ? tc2_prepare(p) : (p.tc2 ? CUI_OK : tc_prepare(p));
     if (s != CUI_OK) return s;
     plan->p.precision = 1;
     return CUI_OK;

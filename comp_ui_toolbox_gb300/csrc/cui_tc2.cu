@@ -1,0 +1,965 @@
+// Line-unit split-BF16 tensor-core (tcgen05) contractions of the Born operator
+// for 2D setups with 4 grid points per element pitch.
+//
+// Table row of frequency f and depth z: T[o], o = x + 4*e' (x grid index,
+// e' = E-1-e reversed element index; the lateral-offset table restated from
+// setup_grid_symmetric.m:175-232).  Shifting the element by one moves the row
+// window by 4 complex entries = 16 bytes, which is exactly the row pitch of a
+// canonical no-swizzle K-major core matrix.  So the raw row, packed as bf16x2
+// (re, im) words, *is* the forward's A operand over a whole grid line:
+//     A[e'][x] = T[x + 4e']      descriptor LBO = 16 B, SBO = 128 B
+// and no operand has to be expanded.  The adjoint contracts over elements
+// (K = e') with rows = points of one residue class x = r + 4j, whose rows shift
+// by one entry; it expands each residue into 16-byte "spread chunks" (chunk i =
+// T[r+4i], T[r+4(i+1)], T[r+4(i+2)], T[r+4(i+3)]) with LBO = 64 B, SBO = 128 B.
+//
+// Columns of the B operand are (slot, object) pairs of one frequency: every
+// incident wave of the frequency times a group of right-hand sides, so batched
+// objects share each staged table row.  Complex arithmetic: K interleaves
+// (re, im); B is stacked along N as [B1 hi | B2 hi | B1 lo | B2 lo] (NT columns
+// each) with B1/B2 the two real forms that give Re and Im of the product.  Per
+// K step one MMA with A hi (N = 4NT) and one with A lo (N = 2NT, accumulating
+// onto the hi x hi columns) form hi*hi + lo*hi + hi*lo in FP32 tensor memory.
+// Every accumulation chain covers 16 K steps and is then added into FP32
+// registers (the forward) or multiplied into the gradient (the adjoint).
+//
+// Block: 8 producer warps (operand staging, tensor-memory read-out, epilogue),
+// one warp whose lane 0 issues the MMAs and one whose lane 0 issues the bulk
+// copies (table rows, incident-field and gamma segments) several stages ahead,
+// so that no producer ever waits on global memory.  Stages are handed over with
+// mbarriers; every wait has a wall-clock limit after which the block drains its
+// asynchronous work, raises the plan's status word and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+
+#include "cui_internal.cuh"
+#include "cui_tc.cuh"
+
+namespace cui {
+namespace {
+
+constexpr int kProd = 256;                 // producer threads (warps 0-7)
+constexpr int kThreads2 = kProd + 64;      // + the MMA warp and the bulk-copy warp
+constexpr int kKC = 64;                    // forward: grid points per pipeline stage
+constexpr int kChainChunks = 2;            // forward: stages per accumulation chain (2 x 8 K steps)
+constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s per wait
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// hi/lo split of (a, b): hi = bf16(a, b), lo = bf16(a - hi, b - hi)
+__device__ __forceinline__ void split(float a, float b, uint32_t& hi, uint32_t& lo) {
+    hi = pack2(a, b);
+    const float ha = __uint_as_float(hi << 16), hb = __uint_as_float(hi & 0xFFFF0000u);
+    lo = pack2(a - ha, b - hb);
+}
+
+// (x, y) -> (-y, x) on a packed bf16x2 word: swap halves, negate the new low half
+__device__ __forceinline__ uint32_t rot(uint32_t w) { return __byte_perm(w, 0, 0x1032) ^ 0x00008000u; }
+
+__device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+
+// wait by every lane of a producer warp; the result is made warp-uniform so that
+// the warp-wide tcgen05.ld that follows is always executed by all 32 lanes
+__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    const bool ok = tc::bar_wait_abortable(bar, parity, abort_flag, kWaitLimitNs);
+    return __all_sync(0xffffffffu, ok);
+}
+
+// named barrier over the 256 producer threads
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// byte offset of B row `row`, K group `g` (4 complex = 16 B) in a K-major stage
+// whose 8-row groups are `sbo` bytes apart
+__device__ __forceinline__ uint32_t b_off(int row, int g, int sbo) {
+    return static_cast<uint32_t>((row >> 3) * sbo + g * 128 + (row & 7) * 16);
+}
+
+// ---------------------------------------------------------------------------
+// band rows: tr[v][f][z][o], v = hi/lo of the packed (re, im) table entry
+// ---------------------------------------------------------------------------
+__global__ void row_kernel(const float2* __restrict__ table, uint32_t* __restrict__ tr, int64_t n_rows, int Nox,
+                           int RowW, int64_t vstride) {
+    const int64_t n = n_rows * RowW;
+    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
+         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t row = idx / RowW;
+        const int o = static_cast<int>(idx - row * RowW);
+        const float2 v = (o < Nox) ? table[row * Nox + o] : make_float2(0.f, 0.f);
+        uint32_t hi, lo;
+        split(v.x, v.y, hi, lo);
+        tr[idx] = hi;
+        tr[vstride + idx] = lo;
+    }
+}
+
+// Column tiles: Bt == 1 -> column c is slot c of the frequency (ns <= NT), one
+// object; Bt == 2 -> the column halves hold objects b0 and b0+1, column
+// c = h*NT/2 + slot (ns <= NT/2).  Returns the slot index (-1: unused) and object.
+template <int NT>
+__device__ __forceinline__ void column(int c, int ns, int s0, int b0, int Bt, int B, const int* __restrict__ f_slot_list,
+                                       int& slot, int& b) {
+    const int bl = (Bt == 2 && c >= NT / 2) ? 1 : 0;
+    const int sl = c - bl * (NT / 2);
+    b = b0 + bl;
+    slot = (sl < ns && b < B) ? __ldg(f_slot_list + s0 + sl) : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Forward: D[e'][c] = sum over the block's grid lines and points x of
+//   T_{f,z}[x + 4e'] q_c(x),   q_c = p_in[slot_c] * gamma[b_c]
+// A = band row (M = 128 element rows), B = q (N = 4NT stacked rows), K = x.
+// B1 = conj(q) = (q_re, -q_im) gives Re(T q), B2 = (q_im, q_re) gives Im(T q).
+// The bulk-copy warp brings, per stage of 64 points, the incident-field
+// segments of every slot of f and the gamma segments of the tile's objects
+// ("raw" stages); producers multiply them, split to bf16 hi/lo and store B.
+// ---------------------------------------------------------------------------
+constexpr int kRawRow = 64 * 8 + 16;  // bytes per incident-field row of a raw stage (16 B pad: no bank conflicts)
+
+struct Fwd2Args {
+    const uint32_t* tr;
+    int64_t tr_vstride;
+    int RowW, RBW;
+    const float2* p_in;
+    const float2* gamma;  // 16-byte aligned, even leading dimension
+    int64_t ldg;
+    const int* f_slot_ptr;
+    const int* f_slot_list;
+    int Nx, Nz, Ex, E, S, B, Bt, ms;  // ms: most slots of any frequency (rows of a raw stage)
+    int64_t P;
+    int lines_per_group, n_lines;
+    float2* part;  // [groups][S][B][E]
+    int* status;
+};
+
+template <int NT>
+struct FwdCfg {
+    static constexpr int NS = NT >= 32 ? 3 : 4;  // B stages
+    static constexpr int NR = 4;                 // raw stages
+    static constexpr int STB = NT * 1024;        // 4NT rows x 64 points x 4 B
+    static constexpr int SBO = 2048;             // 8-row groups: 16 K groups x 128 B
+    static constexpr uint32_t TCOLS = 8 * NT;    // 2 accumulators x 4NT columns
+    static constexpr int ITEMS = NT / 16;        // (4 points, column) items per producer
+    static constexpr int LAG = NS - 1;           // read-out trails staging by LAG stages
+};
+
+template <int NT>
+struct FwdLayout {
+    int RS, oRaw, oBand, oBar;
+    size_t total;
+    __host__ __device__ FwdLayout(int ms, int Bt, int RBW) {
+        using C = FwdCfg<NT>;
+        RS = (ms * kRawRow + Bt * 512 + 15) & ~15;
+        oRaw = C::NS * C::STB;
+        oBand = oRaw + C::NR * RS;
+        oBar = oBand + 16 * RBW;
+        total = static_cast<size_t>(oBar) + 8 * (2 * C::NS + 2 * C::NR + 9) + 16;
+    }
+};
+
+template <int NT>
+__global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a) {
+    using C = FwdCfg<NT>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const FwdLayout<NT> L(a.ms, a.Bt, a.RBW);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = blockIdx.x, f = blockIdx.y;
+    const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+    const int b0 = blockIdx.z * a.Bt;
+    const int line0 = grp * a.lines_per_group, line1 = min(line0 + a.lines_per_group, a.n_lines);
+    if (ns == 0 || b0 >= a.B || line0 >= line1) return;  // uniform over the block
+    // a block of an earlier launch gave up (status not yet read): skip the work, keep the error
+    if (__syncthreads_or(tid == 0 && (*reinterpret_cast<volatile int*>(a.status) & 6) != 0)) return;
+    const int nb = min(a.Bt, a.B - b0);
+    const int nL = line1 - line0;
+    const int nKC = (a.Nx + kKC - 1) / kKC;
+    const int Q = nL * nKC;
+
+    const uint32_t sB = tc::smem_u32(smem);
+    const uint32_t sRaw = sB + L.oRaw, sBand = sB + L.oBand;
+    const uint32_t bar0 = sB + L.oBar;
+    const uint32_t FULL = bar0, EMPTY = bar0 + 8 * C::NS, RAWF = bar0 + 16 * C::NS, RAWE = RAWF + 8 * C::NR,
+                   ACCF = RAWF + 16 * C::NR, ACCE = ACCF + 16, BANDF = ACCF + 32, BANDE = ACCF + 48, DRAIN = ACCF + 64;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NS + 2 * C::NR + 9));
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+
+    if (tid == 0) {
+        for (int s = 0; s < C::NS; ++s) {
+            tc::bar_init(FULL + 8 * s, kProd);
+            tc::bar_init(EMPTY + 8 * s, 1);
+        }
+        for (int s = 0; s < C::NR; ++s) {
+            tc::bar_init(RAWF + 8 * s, 1);
+            tc::bar_init(RAWE + 8 * s, kProd);
+        }
+        for (int k = 0; k < 2; ++k) {
+            tc::bar_init(ACCF + 8 * k, 1);
+            tc::bar_init(ACCE + 8 * k, kProd);
+            tc::bar_init(BANDF + 8 * k, 1);
+            tc::bar_init(BANDE + 8 * k, 1);
+        }
+        tc::bar_init(DRAIN, 1);
+        *abort_flag = 0;
+    }
+    if (tid < kProd) {  // zero the row buffers beyond the copied entries (read by rows e' >= E)
+        const int tail = a.RBW - a.RowW;
+        for (int i = tid; i < 4 * tail; i += kProd) {
+            const int buf = i / tail, o = a.RowW + (i - buf * tail);
+            *reinterpret_cast<uint32_t*>(smem + L.oBand + (static_cast<size_t>(buf) * a.RBW + o) * 4) = 0u;
+        }
+        tc::fence_async_smem();
+    }
+    if (warp == 8) tc::tmem_alloc(tc::smem_u32(tslot), C::TCOLS);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    int zero = 0;
+
+    if (warp == 8) {
+        if (lane == 0) {  // ---- MMA issue ----
+            bool ok = true;
+            constexpr uint32_t id_hi = tc::idesc_bf16(128, 4 * NT), id_lo = tc::idesc_bf16(128, 2 * NT);
+            for (int q = 0; q < Q; ++q) {
+                const int li = q / nKC, kc = q - li * nKC, bb = li & 1;
+                if (kc == 0 && !(ok = tc::bar_wait_abortable(BANDF + 8 * bb, (li >> 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                const int s = q % C::NS;
+                if (!(ok = tc::bar_wait_abortable(FULL + 8 * s, (q / C::NS) & 1, abort_flag, kWaitLimitNs))) break;
+                const int k = q / kChainChunks, acc = k & 1;
+                const bool first = (q % kChainChunks) == 0;
+                if (first && k >= 2 &&
+                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((k >> 1) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                tc::fence_after_sync();
+                const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
+                const int x0 = kc * kKC;
+                const int nk = min(8, (a.Nx - x0) / 8);
+                const uint32_t ahi = sBand + (bb * 2 + 0) * a.RBW * 4u + 4u * x0;
+                const uint32_t alo = sBand + (bb * 2 + 1) * a.RBW * 4u + 4u * x0;
+                const uint32_t bst = sB + s * C::STB;
+                for (int ks = 0; ks < nk; ++ks) {
+                    const uint64_t dh = tc::smem_desc(ahi + 32u * ks, 16, 128);
+                    const uint64_t dl = tc::smem_desc(alo + 32u * ks, 16, 128);
+                    const uint64_t db = tc::smem_desc(bst + 256u * ks, 128, C::SBO);
+                    tc::mma_bf16(td, dh, db, id_hi, (first && ks == 0) ? 0u : 1u);
+                    tc::mma_bf16(td, dl, db, id_lo, 1u);
+                }
+                tc::commit(EMPTY + 8 * s);
+                if (q % kChainChunks == kChainChunks - 1 || q == Q - 1) tc::commit(ACCF + 8 * acc);
+                if (kc == nKC - 1) tc::commit(BANDE + 8 * bb);
+            }
+            tc::commit(DRAIN);
+            tc::bar_wait_abortable(DRAIN, 0, &zero, kWaitLimitNs);
+            if (!ok) atomicOr(a.status, 2);
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {  // ---- bulk copies: table rows per line, raw inputs per stage ----
+            bool ok = true;
+            int last_raw[C::NR], last_band[2] = {-1, -1};
+#pragma unroll
+            for (int s = 0; s < C::NR; ++s) last_raw[s] = -1;
+            auto band = [&](int li) {
+                const int bb = li & 1;
+                const uint32_t bytes = 4u * a.RowW;
+                tc::bar_expect_tx(BANDF + 8 * bb, 2 * bytes);
+                const int64_t row = static_cast<int64_t>(f) * a.Nz + (line0 + li);
+                for (int v = 0; v < 2; ++v)
+                    tc::bulk_g2s(sBand + (bb * 2 + v) * a.RBW * 4u, a.tr + v * a.tr_vstride + row * a.RowW, bytes,
+                                 BANDF + 8 * bb);
+                last_band[bb] = li >> 1;
+            };
+            band(0);
+            if (nL > 1) band(1);
+            const int bpos = min(nKC - 1, C::NR);
+            for (int q = 0; q < Q; ++q) {
+                const int li = q / nKC, kc = q - li * nKC;
+                // rows of line li+1 go into the buffer of line li-1 once its MMAs are done
+                if (kc == bpos && li >= 1 && li + 1 < nL) {
+                    if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((li + 1) & 1), (((li + 1) >> 1) - 1) & 1, abort_flag,
+                                                      kWaitLimitNs)))
+                        break;
+                    band(li + 1);
+                }
+                const int rs = q % C::NR;
+                if (q >= C::NR &&
+                    !(ok = tc::bar_wait_abortable(RAWE + 8 * rs, ((q / C::NR) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                const int x0 = kc * kKC;
+                const uint32_t seg = 8u * min(kKC, a.Nx - x0);
+                tc::bar_expect_tx(RAWF + 8 * rs, (ns + nb) * seg);
+                const int64_t pt = static_cast<int64_t>(line0 + li) * a.Nx + x0;
+                const uint32_t dst = sRaw + rs * L.RS;
+                for (int sl = 0; sl < ns; ++sl) {
+                    const int slot = __ldg(a.f_slot_list + s0 + sl);
+                    tc::bulk_g2s(dst + sl * kRawRow, a.p_in + static_cast<int64_t>(slot) * a.P + pt, seg, RAWF + 8 * rs);
+                }
+                for (int bl = 0; bl < nb; ++bl)
+                    tc::bulk_g2s(dst + a.ms * kRawRow + bl * 512, a.gamma + static_cast<int64_t>(b0 + bl) * a.ldg + pt, seg,
+                                 RAWF + 8 * rs);
+                last_raw[rs] = q / C::NR;
+            }
+            // every copy issued must have landed before the block may exit
+            for (int s = 0; s < C::NR; ++s)
+                if (last_raw[s] >= 0) tc::bar_wait_abortable(RAWF + 8 * s, last_raw[s] & 1, &zero, kWaitLimitNs);
+            for (int k = 0; k < 2; ++k)
+                if (last_band[k] >= 0) tc::bar_wait_abortable(BANDF + 8 * k, last_band[k] & 1, &zero, kWaitLimitNs);
+            if (!ok) atomicOr(a.status, 2);
+        }
+    } else {
+        // ---- producers: q = p_in * gamma -> B stages; accumulator read-out ----
+        const int qd = warp & 3, h = warp >> 2;
+        int cc[C::ITEMS], g4[C::ITEMS], prow[C::ITEMS], grow[C::ITEMS];
+#pragma unroll
+        for (int it = 0; it < C::ITEMS; ++it) {
+            const int ib = warp + 8 * it, cb = ib % (NT / 8), gb = ib / (NT / 8);
+            cc[it] = 8 * cb + (lane & 7);
+            g4[it] = 4 * gb + (lane >> 3);
+            const int bl = (a.Bt == 2 && cc[it] >= NT / 2) ? 1 : 0, sl = cc[it] - bl * (NT / 2);
+            const bool valid = sl < ns && bl < nb;
+            prow[it] = valid ? sl * kRawRow + 32 * g4[it] : -1;
+            grow[it] = valid ? a.ms * kRawRow + bl * 512 + 32 * g4[it] : -1;
+        }
+        float acc[NT];
+#pragma unroll
+        for (int c = 0; c < NT; ++c) acc[c] = 0.f;
+        const uint32_t lane_addr = static_cast<uint32_t>(qd * 32) << 16;
+        bool ok = true;
+        for (int q = 0; q < Q + C::LAG && ok; ++q) {
+            if (q < Q) {
+                const int rs = q % C::NR, s = q % C::NS;
+                const int kc = q % nKC;
+                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag))) break;
+                const uint32_t raw = sRaw + rs * L.RS;
+                float4 pv[C::ITEMS][2], gv[C::ITEMS][2];
+#pragma unroll
+                for (int it = 0; it < C::ITEMS; ++it) {
+                    const bool in = prow[it] >= 0 && kc * kKC + 4 * g4[it] < a.Nx;
+                    if (in) {
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(pv[it][0].x), "=f"(pv[it][0].y), "=f"(pv[it][0].z), "=f"(pv[it][0].w)
+                                     : "r"(raw + prow[it]) : "memory");
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(pv[it][1].x), "=f"(pv[it][1].y), "=f"(pv[it][1].z), "=f"(pv[it][1].w)
+                                     : "r"(raw + prow[it] + 16) : "memory");
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(gv[it][0].x), "=f"(gv[it][0].y), "=f"(gv[it][0].z), "=f"(gv[it][0].w)
+                                     : "r"(raw + grow[it]) : "memory");
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(gv[it][1].x), "=f"(gv[it][1].y), "=f"(gv[it][1].z), "=f"(gv[it][1].w)
+                                     : "r"(raw + grow[it] + 16) : "memory");
+                    } else {
+                        pv[it][0] = pv[it][1] = gv[it][0] = gv[it][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                }
+                tc::bar_arrive(RAWE + 8 * rs);
+                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag))) break;
+                const uint32_t bst = sB + s * C::STB;
+#pragma unroll
+                for (int it = 0; it < C::ITEMS; ++it) {
+                    const float pr[4] = {pv[it][0].x, pv[it][0].z, pv[it][1].x, pv[it][1].z};
+                    const float pi[4] = {pv[it][0].y, pv[it][0].w, pv[it][1].y, pv[it][1].w};
+                    const float gr[4] = {gv[it][0].x, gv[it][0].z, gv[it][1].x, gv[it][1].z};
+                    const float gi[4] = {gv[it][0].y, gv[it][0].w, gv[it][1].y, gv[it][1].w};
+                    uint32_t h1[4], l1[4];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const float qx = pr[t] * gr[t] - pi[t] * gi[t], qy = pr[t] * gi[t] + pi[t] * gr[t];
+                        split(qx, -qy, h1[t], l1[t]);  // B1 = (q_re, -q_im); B2 = rot(B1) = (q_im, q_re)
+                    }
+                    const int c = cc[it], g = g4[it];
+                    sts128(bst + b_off(c, g, C::SBO), h1[0], h1[1], h1[2], h1[3]);
+                    sts128(bst + b_off(NT + c, g, C::SBO), rot(h1[0]), rot(h1[1]), rot(h1[2]), rot(h1[3]));
+                    sts128(bst + b_off(2 * NT + c, g, C::SBO), l1[0], l1[1], l1[2], l1[3]);
+                    sts128(bst + b_off(3 * NT + c, g, C::SBO), rot(l1[0]), rot(l1[1]), rot(l1[2]), rot(l1[3]));
+                }
+                tc::fence_async_smem();
+                tc::bar_arrive(FULL + 8 * s);
+            }
+            const int qr = q - C::LAG;
+            if (qr >= 0 && (qr % kChainChunks == kChainChunks - 1 || qr == Q - 1)) {
+                const int k = qr / kChainChunks, accs = k & 1;
+                if (!(ok = warp_wait(ACCF + 8 * accs, (k >> 1) & 1, abort_flag))) break;
+                tc::fence_after_sync();
+                const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NT);
+#pragma unroll
+                for (int jj = 0; jj < NT / 16; ++jj) {
+                    float v1[16], v2[16];
+                    tc::tmem_ld16(col + 16 * jj, v1);
+                    tc::tmem_ld16(col + 2 * NT + 16 * jj, v2);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) acc[16 * jj + u] += v1[u] + v2[u];
+                }
+                tc::fence_before_sync();
+                tc::bar_arrive(ACCE + 8 * accs);
+            }
+        }
+        if (ok) {
+            const int ep = qd * 32 + lane, e = a.Ex - 1 - ep;
+            if (e >= 0) {
+                float* out = reinterpret_cast<float*>(a.part);
+#pragma unroll
+                for (int c = 0; c < NT; ++c) {
+                    int sl, b;
+                    column<NT>(c, ns, s0, b0, a.Bt, a.B, a.f_slot_list, sl, b);
+                    if (sl >= 0)
+                        out[2 * (((static_cast<int64_t>(grp) * a.S + sl) * a.B + b) * a.E + e) + h] = acc[c];
+                }
+            }
+        } else {
+            atomicOr(a.status, 2);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 8) {
+        __syncwarp();
+        tc::tmem_dealloc(tmem, C::TCOLS);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of one grid line z, residue r (x = r + 4j) and frequency f:
+//   Z[j][c] = sum_e' conj(T[r + 4(j + e')]) V[e'][c]
+//   gamma_hat[b_c](x) += conj(p_in[slot_c](x)) Z[j][c]
+// A = spread chunks of residue r (M = 128 point rows j, K = elements e'),
+// B = V columns (N = 4NT stacked rows), loaded once per frequency.
+// B1 = (V_re, V_im) gives Re(conj(T) V); B2 = rot(B1) = (-V_im, V_re) gives -Im.
+// The epilogue reads the incident fields of the unit from a residue-major copy
+// (p_rm[slot][z][r][j]) that the bulk-copy warp brings in ahead of time, and
+// keeps gamma_hat of its 4 points in registers for the whole frequency chunk.
+// ---------------------------------------------------------------------------
+struct Adj2Args {
+    const uint32_t* tr;
+    int64_t tr_vstride;
+    int RowW, RBW;
+    const float2* p_rm;  // [S][Nz][4][Jp]
+    int Jp;
+    const float2* V;     // [S][B][E]
+    const int* f_slot_ptr;
+    const int* f_slot_list;
+    int Nx, Nz, Ex, E, Epad, B, Bt, F, fchunk, ms;
+    int64_t P;
+    float2* part;        // [nfc][B][P]
+    int* status;
+};
+
+template <int NT>
+struct AdjCfg {
+    static constexpr int NA = 3;               // spread-chunk stages
+    static constexpr int NP = 3;               // incident-field stages
+    static constexpr uint32_t TCOLS = 8 * NT;  // 2 accumulators x 4NT columns
+    static constexpr int LAG = 2;              // the epilogue trails the spreading by 2 units
+};
+
+template <int NT>
+struct AdjLayout {  // byte offsets of the dynamic shared memory
+    int NCH, BB, AB, PS, oA, oP, oBand, oF, oBar;
+    size_t total;
+    __host__ __device__ AdjLayout(int Epad, int RBW, int ms, int Jp, int fchunk) {
+        using C = AdjCfg<NT>;
+        NCH = 128 + Epad;
+        BB = 16 * NT * Epad;
+        AB = 2 * NCH * 16;
+        PS = ms * Jp * 8;
+        oA = 2 * BB;
+        oP = oA + C::NA * AB;
+        oBand = oP + C::NP * PS;
+        oF = oBand + 16 * RBW;
+        oBar = (oF + 4 * fchunk + 7) & ~7;
+        total = static_cast<size_t>(oBar) + 8 * (2 * C::NA + 2 * C::NP + 13) + 16;
+    }
+};
+
+template <int NT>
+__global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a) {
+    using C = AdjCfg<NT>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int z = blockIdx.x, fc = blockIdx.y;
+    const int b0 = blockIdx.z * a.Bt;
+    if (b0 >= a.B) return;  // uniform
+    if (__syncthreads_or(tid == 0 && (*reinterpret_cast<volatile int*>(a.status) & 6) != 0)) return;
+    const int f_lo = fc * a.fchunk, f_hi = min(f_lo + a.fchunk, a.F);
+
+    const uint32_t sbase = tc::smem_u32(smem);
+    const uint32_t sBv = sbase, sA = sbase + L.oA, sP = sbase + L.oP, sBand = sbase + L.oBand;
+    int* sF = reinterpret_cast<int*>(smem + L.oF);
+    const uint32_t bar0 = sbase + L.oBar;
+    const uint32_t BFULL = bar0, BEMPTY = bar0 + 16, AFULL = bar0 + 32, AEMPTY = AFULL + 8 * C::NA,
+                   PF = AFULL + 16 * C::NA, PE = PF + 8 * C::NP, ACCF = PF + 16 * C::NP, ACCE = ACCF + 16,
+                   BANDF = ACCF + 32, BANDE = ACCF + 48, DRAIN = ACCF + 64;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NA + 2 * C::NP + 13));
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+    volatile int* nfa_s = reinterpret_cast<volatile int*>(tslot + 2);
+
+    if (tid == 0) {
+        for (int k = 0; k < 2; ++k) {
+            tc::bar_init(BFULL + 8 * k, kProd);
+            tc::bar_init(BEMPTY + 8 * k, 1);
+            tc::bar_init(ACCF + 8 * k, 1);
+            tc::bar_init(ACCE + 8 * k, kProd);
+            tc::bar_init(BANDF + 8 * k, 1);
+            tc::bar_init(BANDE + 8 * k, kProd);
+        }
+        for (int s = 0; s < C::NA; ++s) {
+            tc::bar_init(AFULL + 8 * s, kProd);
+            tc::bar_init(AEMPTY + 8 * s, 1);
+        }
+        for (int s = 0; s < C::NP; ++s) {
+            tc::bar_init(PF + 8 * s, 1);
+            tc::bar_init(PE + 8 * s, kProd);
+        }
+        tc::bar_init(DRAIN, 1);
+        *abort_flag = 0;
+        int n = 0;
+        for (int f = f_lo; f < f_hi; ++f)
+            if (a.f_slot_ptr[f + 1] > a.f_slot_ptr[f]) sF[n++] = f;
+        *nfa_s = n;
+    }
+    if (tid < kProd) {
+        const int tail = a.RBW - a.RowW;
+        for (int i = tid; i < 4 * tail; i += kProd) {
+            const int buf = i / tail, o = a.RowW + (i - buf * tail);
+            *reinterpret_cast<uint32_t*>(smem + L.oBand + (static_cast<size_t>(buf) * a.RBW + o) * 4) = 0u;
+        }
+    }
+    if (warp == 8) tc::tmem_alloc(tc::smem_u32(tslot), C::TCOLS);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const int nfa = *nfa_s;
+    const int U = 4 * nfa;
+    const int NCH = L.NCH;
+    const int SBOB = 32 * a.Epad;
+    int zero = 0;
+
+    if (warp == 8) {
+        if (lane == 0) {  // ---- MMA issue ----
+            bool ok = true;
+            constexpr uint32_t id_hi = tc::idesc_bf16(128, 4 * NT), id_lo = tc::idesc_bf16(128, 2 * NT);
+            const int ksteps = a.Epad / 8;
+            for (int u = 0; u < U; ++u) {
+                const int fi = u >> 2, r = u & 3, bb = fi & 1;
+                if (r == 0 && !(ok = tc::bar_wait_abortable(BFULL + 8 * bb, (fi >> 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                const int sa = u % C::NA;
+                if (!(ok = tc::bar_wait_abortable(AFULL + 8 * sa, (u / C::NA) & 1, abort_flag, kWaitLimitNs))) break;
+                const int acc = u & 1;
+                if (u >= 2 && !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((u >> 1) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                tc::fence_after_sync();
+                const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
+                const uint32_t ah = sA + sa * L.AB, al = ah + NCH * 16, bv = sBv + bb * L.BB;
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint64_t dh = tc::smem_desc(ah + 128u * ks, 64, 128);
+                    const uint64_t dl = tc::smem_desc(al + 128u * ks, 64, 128);
+                    const uint64_t db = tc::smem_desc(bv + 256u * ks, 128, SBOB);
+                    tc::mma_bf16(td, dh, db, id_hi, ks > 0 ? 1u : 0u);
+                    tc::mma_bf16(td, dl, db, id_lo, 1u);
+                }
+                tc::commit(AEMPTY + 8 * sa);
+                tc::commit(ACCF + 8 * acc);
+                if (r == 3) tc::commit(BEMPTY + 8 * bb);
+            }
+            tc::commit(DRAIN);
+            tc::bar_wait_abortable(DRAIN, 0, &zero, kWaitLimitNs);
+            if (!ok) atomicOr(a.status, 4);
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {  // ---- bulk copies: table rows per frequency, incident fields per unit ----
+            bool ok = true;
+            int last_p[C::NP], last_band[2] = {-1, -1};
+#pragma unroll
+            for (int s = 0; s < C::NP; ++s) last_p[s] = -1;
+            auto band = [&](int fi) {
+                const int bb = fi & 1;
+                const uint32_t bytes = 4u * a.RowW;
+                tc::bar_expect_tx(BANDF + 8 * bb, 2 * bytes);
+                const int64_t row = static_cast<int64_t>(sF[fi]) * a.Nz + z;
+                for (int v = 0; v < 2; ++v)
+                    tc::bulk_g2s(sBand + (bb * 2 + v) * a.RBW * 4u, a.tr + v * a.tr_vstride + row * a.RowW, bytes,
+                                 BANDF + 8 * bb);
+                last_band[bb] = fi >> 1;
+            };
+            if (nfa > 0) band(0);
+            if (nfa > 1) band(1);
+            const uint32_t seg = 8u * a.Jp;
+            for (int u = 0; u < U; ++u) {
+                const int fi = u >> 2, r = u & 3;
+                const int pu = u % C::NP;
+                if (u >= C::NP &&
+                    !(ok = tc::bar_wait_abortable(PE + 8 * pu, ((u / C::NP) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    break;
+                // rows of frequency fi+1 go into the buffer of fi-1 once the producers have spread it
+                if (r == 0 && fi >= 1 && fi + 1 < nfa) {
+                    if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((fi + 1) & 1), (((fi + 1) >> 1) - 1) & 1, abort_flag,
+                                                      kWaitLimitNs)))
+                        break;
+                    band(fi + 1);
+                }
+                const int f = sF[fi];
+                const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+                tc::bar_expect_tx(PF + 8 * pu, ns * seg);
+                for (int sl = 0; sl < ns; ++sl) {
+                    const int slot = __ldg(a.f_slot_list + s0 + sl);
+                    tc::bulk_g2s(sP + pu * L.PS + sl * seg,
+                                 a.p_rm + ((static_cast<int64_t>(slot) * a.Nz + z) * 4 + r) * a.Jp, seg, PF + 8 * pu);
+                }
+                last_p[pu] = u / C::NP;
+            }
+            for (int s = 0; s < C::NP; ++s)
+                if (last_p[s] >= 0) tc::bar_wait_abortable(PF + 8 * s, last_p[s] & 1, &zero, kWaitLimitNs);
+            for (int k = 0; k < 2; ++k)
+                if (last_band[k] >= 0) tc::bar_wait_abortable(BANDF + 8 * k, last_band[k] & 1, &zero, kWaitLimitNs);
+            if (!ok) atomicOr(a.status, 4);
+        }
+    } else {
+        const int qd = warp & 3, h = warp >> 2;
+        const int j = qd * 32 + lane;
+        const uint32_t lane_addr = static_cast<uint32_t>(qd * 32) << 16;
+        constexpr int NH = NT / 2;
+        // the half's object and its first slot column: Bt == 1 -> both halves serve object b0
+        const int hb = (a.Bt == 2) ? h : 0, hs = (a.Bt == 2) ? 0 : h * NH;
+        const bool hvalid = b0 + hb < a.B;
+        float gx[4], gy[4];  // gamma_hat of x = r + 4j for the half's object
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) gx[rr] = gy[rr] = 0.f;
+        bool ok = true;
+        for (int it = 0; it < U + C::LAG && ok; ++it) {
+            if (it < U) {
+                const int fi = it >> 2, r = it & 3, bb = fi & 1;
+                if (r == 0) {
+                    const int f = sF[fi];
+                    const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+                    if (fi >= 2 && !(ok = warp_wait(BEMPTY + 8 * bb, ((fi >> 1) - 1) & 1, abort_flag))) break;
+                    // ---- V tile of frequency f -> B buffer bb ----
+                    const uint32_t bv = sBv + bb * L.BB;
+                    const int nblk = (NT / 8) * (a.Epad / 16);
+                    for (int ib = warp; ib < nblk; ib += 8) {
+                        const int cb = ib % (NT / 8), gb = ib / (NT / 8);
+                        const int c = 8 * cb + (lane & 7), g = 4 * gb + (lane >> 3);
+                        int sl, b;
+                        column<NT>(c, ns, s0, b0, a.Bt, a.B, a.f_slot_list, sl, b);
+                        uint32_t hw[4], lw[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const int e = a.Ex - 1 - (4 * g + t);
+                            float2 v = make_float2(0.f, 0.f);
+                            if (sl >= 0 && e >= 0) v = __ldg(a.V + (static_cast<int64_t>(sl) * a.B + b) * a.E + e);
+                            split(v.x, v.y, hw[t], lw[t]);
+                        }
+                        sts128(bv + b_off(c, g, SBOB), hw[0], hw[1], hw[2], hw[3]);
+                        sts128(bv + b_off(NT + c, g, SBOB), rot(hw[0]), rot(hw[1]), rot(hw[2]), rot(hw[3]));
+                        sts128(bv + b_off(2 * NT + c, g, SBOB), lw[0], lw[1], lw[2], lw[3]);
+                        sts128(bv + b_off(3 * NT + c, g, SBOB), rot(lw[0]), rot(lw[1]), rot(lw[2]), rot(lw[3]));
+                    }
+                    tc::fence_async_smem();
+                    tc::bar_arrive(BFULL + 8 * bb);
+                    if (!(ok = warp_wait(BANDF + 8 * bb, (fi >> 1) & 1, abort_flag))) break;
+                }
+                // ---- spread chunks of residue r -> A stage ----
+                const int sa = it % C::NA;
+                if (it >= C::NA && !(ok = warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag))) break;
+                const uint32_t as = sA + sa * L.AB;
+                for (int idx = tid; idx < 2 * NCH; idx += kProd) {
+                    const int v = idx >= NCH ? 1 : 0, i = idx - v * NCH;
+                    const uint32_t row = sBand + (bb * 2 + v) * a.RBW * 4u + 4u * (r + 4 * i);
+                    sts128(as + 16u * idx, lds32(row), lds32(row + 16), lds32(row + 32), lds32(row + 48));
+                }
+                tc::fence_async_smem();
+                tc::bar_arrive(AFULL + 8 * sa);
+                if (r == 3) tc::bar_arrive(BANDE + 8 * bb);
+            }
+            // ---- epilogue of unit ue ----
+            const int ue = it - C::LAG;
+            if (ue >= 0) {
+                const int fi = ue >> 2, r = ue & 3, accs = ue & 1, pu = ue % C::NP;
+                const int f = sF[fi];
+                const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+                const bool xin = r + 4 * j < a.Nx;
+                if (!(ok = warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag))) break;
+                float2 pv[NH];
+#pragma unroll
+                for (int m = 0; m < NH; ++m) {
+                    const int sl = hs + m;
+                    pv[m] = make_float2(0.f, 0.f);  // unused columns contribute zero
+                    if (sl < ns && hvalid && xin)
+                        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                                     : "=f"(pv[m].x), "=f"(pv[m].y)
+                                     : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
+                }
+                tc::bar_arrive(PE + 8 * pu);
+                if (!(ok = warp_wait(ACCF + 8 * accs, (ue >> 1) & 1, abort_flag))) break;
+                tc::fence_after_sync();
+                const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NH);
+                float d0[NH], d1[NH], d2[NH], d3[NH];
+                if constexpr (NH == 16) {
+                    tc::tmem_ld16(col, d0);
+                    tc::tmem_ld16(col + NT, d1);
+                    tc::tmem_ld16(col + 2 * NT, d2);
+                    tc::tmem_ld16(col + 3 * NT, d3);
+                } else {
+                    tc::tmem_ld8(col, d0);
+                    tc::tmem_ld8(col + NT, d1);
+                    tc::tmem_ld8(col + 2 * NT, d2);
+                    tc::tmem_ld8(col + 3 * NT, d3);
+                }
+                tc::tmem_wait_ld();
+                tc::fence_before_sync();
+                tc::bar_arrive(ACCE + 8 * accs);
+                float sx = 0.f, sy = 0.f;
+#pragma unroll
+                for (int m = 0; m < NH; ++m) {
+                    const float zr = d0[m] + d2[m], zi = -(d1[m] + d3[m]);
+                    const float px = pv[m].x, py = pv[m].y;
+                    sx = fmaf(px, zr, fmaf(py, zi, sx));  // conj(p) * Z
+                    sy = fmaf(px, zi, fmaf(-py, zr, sy));
+                }
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+                    if (rr == r) {
+                        gx[rr] += sx;
+                        gy[rr] += sy;
+                    }
+            }
+        }
+        if (!ok) atomicOr(a.status, 4);
+        // every MMA has completed (the last epilogue waited on it): the B buffers hold the
+        // two halves' gamma_hat, [h][bb][x]
+        producers_sync();
+        float2* sG = reinterpret_cast<float2*>(smem);  // [h][x]
+        const bool good = !*abort_flag;
+        if (good) {
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int x = rr + 4 * j;
+                if (x < a.Nx) sG[static_cast<size_t>(h) * a.Nx + x] = make_float2(gx[rr], gy[rr]);
+            }
+        }
+        producers_sync();
+        if (good) {
+            const int64_t line_pt = static_cast<int64_t>(z) * a.Nx;
+            if (a.Bt == 1) {  // both halves hold parts of object b0
+                for (int x = tid; x < a.Nx; x += kProd) {
+                    const float2 g0 = sG[x], g1 = sG[a.Nx + x];
+                    a.part[(static_cast<int64_t>(fc) * a.B + b0) * a.P + line_pt + x] = make_float2(g0.x + g1.x, g0.y + g1.y);
+                }
+            } else {
+                const int nb = min(2, a.B - b0);
+                for (int idx = tid; idx < nb * a.Nx; idx += kProd) {
+                    const int bl = idx / a.Nx, x = idx - bl * a.Nx;
+                    a.part[(static_cast<int64_t>(fc) * a.B + b0 + bl) * a.P + line_pt + x] = sG[static_cast<size_t>(bl) * a.Nx + x];
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 8) {
+        __syncwarp();
+        tc::tmem_dealloc(tmem, C::TCOLS);
+    }
+}
+
+// incident fields in residue-major order: p_rm[s][z][r][j] = p_in[s][z][r + 4j] (zero past the line)
+__global__ void residue_major_kernel(const float2* __restrict__ p_in, float2* __restrict__ p_rm, int64_t n_lines,
+                                     int Nx, int Jp) {
+    const int64_t n = n_lines * 4 * Jp;
+    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
+         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int j = static_cast<int>(idx % Jp);
+        const int64_t t = idx / Jp;
+        const int r = static_cast<int>(t % 4);
+        const int64_t line = t / 4;  // slot * Nz + z
+        const int x = r + 4 * j;
+        p_rm[idx] = (x < Nx) ? p_in[line * Nx + x] : make_float2(0.f, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int tc2_rbw(const Plan* p) {  // entries of a shared-memory row buffer (both kernels' reach)
+    const int need = std::max({p->RowW, 4 * 127 + p->Nx, 4 * (128 + p->Epad) + 12});
+    return (need + 3) / 4 * 4;
+}
+
+struct Tile2 {
+    int NT, Bt, tiles;
+};
+
+Tile2 tile2(const Plan* p, int B) {
+    Tile2 t;
+    const int ms = std::max(1, p->max_slots_per_f);
+    if (B >= 2 && ms <= 8) {
+        t.NT = 16, t.Bt = 2;
+    } else if (B >= 2 && ms <= 16) {
+        t.NT = 32, t.Bt = 2;
+    } else {
+        t.NT = ms <= 16 ? 16 : 32, t.Bt = 1;
+    }
+    t.tiles = (B + t.Bt - 1) / t.Bt;
+    return t;
+}
+
+template <int NT>
+cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const Tile2& t, cudaStream_t st,
+                        int* groups_out) {
+    cudaError_t e;
+    // the bulk copies of gamma segments need 16-byte aligned rows
+    if ((reinterpret_cast<uintptr_t>(gamma) & 15) != 0 || (ldg & 1) != 0) {
+        if ((e = cudaMemcpy2DAsync(p->ws_galign, sizeof(float2) * p->P, gamma, sizeof(float2) * ldg, sizeof(float2) * p->P,
+                                   B, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+            return e;
+        gamma = p->ws_galign;
+        ldg = p->P;
+    }
+    const int n_lines = p->Nz;
+    const size_t slab = static_cast<size_t>(p->S) * B * p->E * sizeof(float2);
+    int groups = std::max(1, std::min(n_lines, (8 * 152 + p->F * t.tiles - 1) / (p->F * t.tiles)));
+    groups = static_cast<int>(std::max<size_t>(1, std::min<size_t>(groups, p->ws_part_bytes / std::max<size_t>(slab, 1))));
+    const int lpg = (n_lines + groups - 1) / groups;
+    groups = (n_lines + lpg - 1) / lpg;  // every group holds at least one line
+    Fwd2Args a;
+    a.tr = p->tr; a.tr_vstride = p->tr_vstride; a.RowW = p->RowW; a.RBW = tc2_rbw(p);
+    a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.S = p->S; a.B = B; a.Bt = t.Bt;
+    a.ms = std::max(1, p->max_slots_per_f); a.P = p->P;
+    a.lines_per_group = lpg; a.n_lines = n_lines; a.part = p->ws_part; a.status = p->ws_status;
+    const size_t smem = FwdLayout<NT>(a.ms, a.Bt, a.RBW).total;
+    if ((e = cudaFuncSetAttribute(fwd_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem))) != cudaSuccess)
+        return e;
+    if ((e = timing_begin(p, 0, st)) != cudaSuccess) return e;
+    fwd_tc2_kernel<NT><<<dim3(groups, p->F, t.tiles), kThreads2, smem, st>>>(a);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *groups_out = groups;
+    return timing_end(p, st);
+}
+
+template <int NT>
+cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nfc_out) {
+    const size_t slab = static_cast<size_t>(B) * p->P * sizeof(float2);
+    int nfc = std::max(1, std::min(p->F, (8 * 152 + p->Nz * t.tiles - 1) / (p->Nz * t.tiles)));
+    nfc = static_cast<int>(std::max<size_t>(1, std::min<size_t>(nfc, p->ws_part_bytes / std::max<size_t>(slab, 1))));
+    const int fchunk = (p->F + nfc - 1) / nfc;
+    nfc = (p->F + fchunk - 1) / fchunk;
+    Adj2Args a;
+    a.tr = p->tr; a.tr_vstride = p->tr_vstride; a.RowW = p->RowW; a.RBW = tc2_rbw(p);
+    a.p_rm = p->p_rm; a.Jp = p->Jp; a.V = p->ws_G; a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.Epad = p->Epad; a.B = B; a.Bt = t.Bt; a.F = p->F;
+    a.fchunk = fchunk; a.ms = std::max(1, p->max_slots_per_f); a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
+    const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
+    cudaError_t e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(L.total));
+    if (e != cudaSuccess) return e;
+    if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
+    adj_tc2_kernel<NT><<<dim3(p->Nz, nfc, t.tiles), kThreads2, L.total, st>>>(a);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *nfc_out = nfc;
+    return timing_end(p, st);
+}
+
+// largest dynamic shared memory any launch of this plan can request
+size_t tc2_smem_need(const Plan* p, int Epad, int RowW) {
+    Plan q = *p;
+    q.Epad = Epad;
+    q.RowW = RowW;
+    const int rbw = tc2_rbw(&q);
+    const int ms = std::max(1, p->max_slots_per_f);
+    const int Jp = ((p->Nx + 3) / 4 + 1) / 2 * 2;
+    size_t need = 0;
+    for (int B = 1; B <= std::min(p->max_objects, 2); ++B) {
+        const Tile2 t = tile2(p, B);
+        if (t.NT == 16)
+            need = std::max({need, FwdLayout<16>(ms, t.Bt, rbw).total, AdjLayout<16>(Epad, rbw, ms, Jp, p->F).total});
+        else
+            need = std::max({need, FwdLayout<32>(ms, t.Bt, rbw).total, AdjLayout<32>(Epad, rbw, ms, Jp, p->F).total});
+    }
+    return need;
+}
+
+}  // namespace
+
+bool tc2_supported(const Plan* p, std::string* why) {
+    if (p->n_dims != 2) { *why = "line-unit kernels cover 2D setups"; return false; }
+    if (p->ppx != 4) { *why = "line-unit kernels need 4 grid points per element pitch"; return false; }
+    if (p->Ex > 128) { *why = "line-unit kernels cover up to 128 elements"; return false; }
+    if (p->Nx % 8 != 0 || p->Nx > 512) { *why = "line-unit kernels need a lateral grid of 8..512 points, a multiple of 8"; return false; }
+    if (p->max_slots_per_f > 32) { *why = "line-unit kernels cover up to 32 incident waves per frequency"; return false; }
+    // the adjoint's final gamma_hat halves (2 x Nx) reuse its two V buffers (2 x 16 NT Epad bytes)
+    if (16 * p->Nx > 32 * 16 * ((p->Ex + 15) / 16 * 16)) {
+        *why = "lateral grid too wide for the element count of the line-unit kernels";
+        return false;
+    }
+    int smem_optin = 0;
+    if (cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device) != cudaSuccess) {
+        *why = "cudaDeviceGetAttribute failed";
+        return false;
+    }
+    const size_t need = tc2_smem_need(p, (p->Ex + 15) / 16 * 16, (p->Nox + 3) / 4 * 4);
+    if (need > static_cast<size_t>(smem_optin)) { *why = "line-unit staging exceeds shared memory"; return false; }
+    return true;
+}
+
+cui_status tc2_prepare(Plan& p) {
+    if (p.tr) return CUI_OK;
+    p.Epad = (p.Ex + 15) / 16 * 16;
+    p.RowW = (p.Nox + 3) / 4 * 4;
+    p.Jp = ((p.Nx + 3) / 4 + 1) / 2 * 2;  // points per residue, even: 16-byte rows
+    const int64_t n_rows = static_cast<int64_t>(p.F) * p.Nz * p.Noy;
+    p.tr_vstride = n_rows * p.RowW;
+    cui_status st = device_alloc(p, reinterpret_cast<void**>(&p.tr), sizeof(uint32_t) * 2 * p.tr_vstride);
+    if (st != CUI_OK) return st;
+    const int64_t n_lines = static_cast<int64_t>(p.S) * p.Nz;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_rm), sizeof(float2) * n_lines * 4 * p.Jp)) != CUI_OK) return st;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.ws_galign), sizeof(float2) * p.P * p.max_objects)) != CUI_OK)
+        return st;
+    int blocks = static_cast<int>(std::min<int64_t>((p.tr_vstride + 255) / 256, 152 * 32));
+    row_kernel<<<blocks, 256>>>(p.table, p.tr, n_rows, p.Nox, p.RowW, p.tr_vstride);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return check_cuda(e, "band rows");
+    blocks = static_cast<int>(std::min<int64_t>((n_lines * 4 * p.Jp + 255) / 256, 152 * 32));
+    residue_major_kernel<<<blocks, 256>>>(p.p_in, p.p_rm, n_lines, p.Nx, p.Jp);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "residue-major incident fields");
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return check_cuda(e, "line-unit tables");
+    p.tc_bytes += sizeof(uint32_t) * 2 * static_cast<size_t>(p.tr_vstride) + sizeof(float2) * n_lines * 4 * p.Jp +
+                  sizeof(float2) * p.P * p.max_objects;
+    p.tc2 = 1;
+    return CUI_OK;
+}
+
+cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* groups) {
+    const Tile2 t = tile2(p, B);
+    return t.NT == 16 ? launch_fwd2<16>(p, gamma, ldg, B, t, st, groups) : launch_fwd2<32>(p, gamma, ldg, B, t, st, groups);
+}
+
+cudaError_t launch_adj_tc2(Plan* p, int B, cudaStream_t st, int* nfc) {
+    const Tile2 t = tile2(p, B);
+    return t.NT == 16 ? launch_adj2<16>(p, B, t, st, nfc) : launch_adj2<32>(p, B, t, st, nfc);
+}
+
+}  // namespace cui

@@ -309,3 +309,33 @@ def test_bf16x3_refused_for_3d():
     with pytest.raises(CuiError) as ei:
         op.set_precision("bf16x3")
     assert ei.value.status == 2
+
+
+@pytest.mark.parametrize("wname,n_freq,n_obj", [("2d-gradient", 12, 1), ("2d-batched", 3, 8), ("2d-plain", 8, 5)])
+def test_bf16x3_full_lines_match_fp32(wname, n_freq, n_obj):
+    """Split-BF16 tensor-core forward and adjoint on full-width benchmark grid lines
+    (512 or 256 points, 128 elements; several lines per block, several frequencies
+    per block) against the FP32 path of the same plan, which the tests above pin to
+    the FP64 oracle within 2e-7.  Bound: relative L2 <= 1e-5."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload(wname)
+    w.f = w.f[:n_freq]
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
+    rng = np.random.default_rng(3)
+    g = rng.standard_normal((op.n_points, n_obj)) + 1j * rng.standard_normal((op.n_points, n_obj))
+    y = rng.standard_normal((op.n_observations, n_obj)) + 1j * rng.standard_normal((op.n_observations, n_obj))
+    u32 = op.forward(dev(g)).cpu().numpy()
+    a32 = op.adjoint(dev(y)).cpu().numpy()
+    op.set_precision("bf16x3")
+    u16 = op.forward(dev(g)).cpu().numpy()
+    a16 = op.adjoint(dev(y)).cpu().numpy()
+    assert op.device_status() == 0
+    assert rel_l2(u16, u32) <= TOL
+    assert rel_l2(a16, a32) <= TOL
+    # per object, so that a wrong column mapping of one object cannot hide in the total
+    for b in range(n_obj):
+        assert rel_l2(u16[:, b], u32[:, b]) <= TOL
+        assert rel_l2(a16[:, b], a32[:, b]) <= TOL
+    op.close()
