@@ -122,8 +122,14 @@ struct Plan {
     uint32_t* tr = nullptr;
     int64_t tr_vstride = 0;          // entries per variant
     int RowW = 0;                    // entries per row (lateral offsets rounded up to 4, zero padded)
-    float2* p_rm = nullptr;          // incident fields residue-major [S][Nz][4][Jp] (adjoint epilogue)
+    // incident fields re-laid so that one bulk copy brings every slot of a frequency:
+    //   p_fw [F][Nz][nKC][ms][66]  forward: 64-point segments (+2 pad) of each slot of f
+    //   p_ad [F][Nz][4][ms][Jp]    adjoint: residue classes x = r + 4j of each slot of f
+    float2* p_fw = nullptr;
+    float2* p_ad = nullptr;
     int Jp = 0;                      // points per residue class, rounded up to even
+    int nKC = 0;                     // 64-point segments per grid line
+    int ms = 0;                      // slot rows per frequency in both layouts (most slots of any frequency)
     float2* ws_galign = nullptr;     // [max_objects][P] aligned copy of a misaligned gamma (forward)
     int* ws_status = nullptr;        // device status word (bounded waits that gave up)
 

@@ -134,7 +134,7 @@ struct Fwd2Args {
     const uint32_t* tr;
     int64_t tr_vstride;
     int RowW, RBW;
-    const float2* p_in;
+    const float2* p_fw;   // [F][Nz][nKC][ms][66]
     const float2* gamma;  // 16-byte aligned, even leading dimension
     int64_t ldg;
     const int* f_slot_ptr;
@@ -301,13 +301,12 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                     break;
                 const int x0 = kc * kKC;
                 const uint32_t seg = 8u * min(kKC, a.Nx - x0);
-                tc::bar_expect_tx(RAWF + 8 * rs, (ns + nb) * seg);
+                tc::bar_expect_tx(RAWF + 8 * rs, ns * kRawRow + nb * seg);
                 const int64_t pt = static_cast<int64_t>(line0 + li) * a.Nx + x0;
                 const uint32_t dst = sRaw + rs * L.RS;
-                for (int sl = 0; sl < ns; ++sl) {
-                    const int slot = __ldg(a.f_slot_list + s0 + sl);
-                    tc::bulk_g2s(dst + sl * kRawRow, a.p_in + static_cast<int64_t>(slot) * a.P + pt, seg, RAWF + 8 * rs);
-                }
+                // every slot's segment of this stage in one copy
+                tc::bulk_g2s(dst, a.p_fw + ((static_cast<int64_t>(f) * a.Nz + line0 + li) * nKC + kc) * a.ms * (kRawRow / 8),
+                             ns * kRawRow, RAWF + 8 * rs);
                 for (int bl = 0; bl < nb; ++bl)
                     tc::bulk_g2s(dst + a.ms * kRawRow + bl * 512, a.gamma + static_cast<int64_t>(b0 + bl) * a.ldg + pt, seg,
                                  RAWF + 8 * rs);
@@ -366,6 +365,8 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                         pv[it][0] = pv[it][1] = gv[it][0] = gv[it][1] = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
+                // the generic-proxy reads above must be ordered before the next bulk copy (async proxy) into the stage
+                tc::fence_async_smem();
                 tc::bar_arrive(RAWE + 8 * rs);
                 if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag))) break;
                 const uint32_t bst = sB + s * C::STB;
@@ -441,14 +442,14 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
 // B = V columns (N = 4NT stacked rows), loaded once per frequency.
 // B1 = (V_re, V_im) gives Re(conj(T) V); B2 = rot(B1) = (-V_im, V_re) gives -Im.
 // The epilogue reads the incident fields of the unit from a residue-major copy
-// (p_rm[slot][z][r][j]) that the bulk-copy warp brings in ahead of time, and
+// (p_ad[f][z][r][slot of f][j]) that the bulk-copy warp brings in, one copy per unit, and
 // keeps gamma_hat of its 4 points in registers for the whole frequency chunk.
 // ---------------------------------------------------------------------------
 struct Adj2Args {
     const uint32_t* tr;
     int64_t tr_vstride;
     int RowW, RBW;
-    const float2* p_rm;  // [S][Nz][4][Jp]
+    const float2* p_ad;  // [F][Nz][4][ms][Jp]
     int Jp;
     const float2* V;     // [S][B][E]
     const int* f_slot_ptr;
@@ -616,13 +617,10 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                     band(fi + 1);
                 }
                 const int f = sF[fi];
-                const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+                const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
                 tc::bar_expect_tx(PF + 8 * pu, ns * seg);
-                for (int sl = 0; sl < ns; ++sl) {
-                    const int slot = __ldg(a.f_slot_list + s0 + sl);
-                    tc::bulk_g2s(sP + pu * L.PS + sl * seg,
-                                 a.p_rm + ((static_cast<int64_t>(slot) * a.Nz + z) * 4 + r) * a.Jp, seg, PF + 8 * pu);
-                }
+                tc::bulk_g2s(sP + pu * L.PS, a.p_ad + ((static_cast<int64_t>(f) * a.Nz + z) * 4 + r) * a.ms * a.Jp, ns * seg,
+                             PF + 8 * pu);
                 last_p[pu] = u / C::NP;
             }
             for (int s = 0; s < C::NP; ++s)
@@ -706,6 +704,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                                      : "=f"(pv[m].x), "=f"(pv[m].y)
                                      : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
                 }
+                tc::fence_async_smem();  // generic reads before the next bulk copy into this stage
                 tc::bar_arrive(PE + 8 * pu);
                 if (!(ok = warp_wait(ACCF + 8 * accs, (ue >> 1) & 1, abort_flag))) break;
                 tc::fence_after_sync();
@@ -779,18 +778,46 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     }
 }
 
-// incident fields in residue-major order: p_rm[s][z][r][j] = p_in[s][z][r + 4j] (zero past the line)
-__global__ void residue_major_kernel(const float2* __restrict__ p_in, float2* __restrict__ p_rm, int64_t n_lines,
-                                     int Nx, int Jp) {
-    const int64_t n = n_lines * 4 * Jp;
+// incident fields, forward layout: p_fw[f][z][kc][sl][t] = p_in[slot sl of f][z][64kc + t] (zero padded)
+__global__ void slot_major_fwd_kernel(const float2* __restrict__ p_in, const int* __restrict__ f_slot_ptr,
+                                      const int* __restrict__ f_slot_list, float2* __restrict__ p_fw, int F, int Nz, int nKC,
+                                      int ms, int Nx, int64_t P) {
+    constexpr int W = kRawRow / 8;
+    const int64_t n = static_cast<int64_t>(F) * Nz * nKC * ms * W;
     for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
          idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int j = static_cast<int>(idx % Jp);
-        const int64_t t = idx / Jp;
-        const int r = static_cast<int>(t % 4);
-        const int64_t line = t / 4;  // slot * Nz + z
+        int64_t t = idx;
+        const int w = static_cast<int>(t % W); t /= W;
+        const int sl = static_cast<int>(t % ms); t /= ms;
+        const int kc = static_cast<int>(t % nKC); t /= nKC;
+        const int z = static_cast<int>(t % Nz);
+        const int f = static_cast<int>(t / Nz);
+        const int s0 = f_slot_ptr[f], ns = f_slot_ptr[f + 1] - s0;
+        const int x = kc * kKC + w;
+        float2 v = make_float2(0.f, 0.f);
+        if (sl < ns && w < kKC && x < Nx) v = p_in[static_cast<int64_t>(f_slot_list[s0 + sl]) * P + static_cast<int64_t>(z) * Nx + x];
+        p_fw[idx] = v;
+    }
+}
+
+// incident fields, adjoint layout: p_ad[f][z][r][sl][j] = p_in[slot sl of f][z][r + 4j] (zero padded)
+__global__ void slot_major_adj_kernel(const float2* __restrict__ p_in, const int* __restrict__ f_slot_ptr,
+                                      const int* __restrict__ f_slot_list, float2* __restrict__ p_ad, int F, int Nz, int ms,
+                                      int Jp, int Nx, int64_t P) {
+    const int64_t n = static_cast<int64_t>(F) * Nz * 4 * ms * Jp;
+    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
+         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t t = idx;
+        const int j = static_cast<int>(t % Jp); t /= Jp;
+        const int sl = static_cast<int>(t % ms); t /= ms;
+        const int r = static_cast<int>(t % 4); t /= 4;
+        const int z = static_cast<int>(t % Nz);
+        const int f = static_cast<int>(t / Nz);
+        const int s0 = f_slot_ptr[f], ns = f_slot_ptr[f + 1] - s0;
         const int x = r + 4 * j;
-        p_rm[idx] = (x < Nx) ? p_in[line * Nx + x] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (sl < ns && x < Nx) v = p_in[static_cast<int64_t>(f_slot_list[s0 + sl]) * P + static_cast<int64_t>(z) * Nx + x];
+        p_ad[idx] = v;
     }
 }
 
@@ -840,10 +867,10 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
     groups = (n_lines + lpg - 1) / lpg;  // every group holds at least one line
     Fwd2Args a;
     a.tr = p->tr; a.tr_vstride = p->tr_vstride; a.RowW = p->RowW; a.RBW = tc2_rbw(p);
-    a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.p_fw = p->p_fw; a.gamma = gamma; a.ldg = ldg;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.S = p->S; a.B = B; a.Bt = t.Bt;
-    a.ms = std::max(1, p->max_slots_per_f); a.P = p->P;
+    a.ms = p->ms; a.P = p->P;
     a.lines_per_group = lpg; a.n_lines = n_lines; a.part = p->ws_part; a.status = p->ws_status;
     const size_t smem = FwdLayout<NT>(a.ms, a.Bt, a.RBW).total;
     if ((e = cudaFuncSetAttribute(fwd_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -866,9 +893,9 @@ cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nf
     nfc = (p->F + fchunk - 1) / fchunk;
     Adj2Args a;
     a.tr = p->tr; a.tr_vstride = p->tr_vstride; a.RowW = p->RowW; a.RBW = tc2_rbw(p);
-    a.p_rm = p->p_rm; a.Jp = p->Jp; a.V = p->ws_G; a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.p_ad = p->p_ad; a.Jp = p->Jp; a.V = p->ws_G; a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.Epad = p->Epad; a.B = B; a.Bt = t.Bt; a.F = p->F;
-    a.fchunk = fchunk; a.ms = std::max(1, p->max_slots_per_f); a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
+    a.fchunk = fchunk; a.ms = p->ms; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
     cudaError_t e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(L.total));
@@ -932,8 +959,12 @@ cui_status tc2_prepare(Plan& p) {
     p.tr_vstride = n_rows * p.RowW;
     cui_status st = device_alloc(p, reinterpret_cast<void**>(&p.tr), sizeof(uint32_t) * 2 * p.tr_vstride);
     if (st != CUI_OK) return st;
-    const int64_t n_lines = static_cast<int64_t>(p.S) * p.Nz;
-    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_rm), sizeof(float2) * n_lines * 4 * p.Jp)) != CUI_OK) return st;
+    p.ms = std::max(1, p.max_slots_per_f);
+    p.nKC = (p.Nx + kKC - 1) / kKC;
+    const size_t fw_elems = static_cast<size_t>(p.F) * p.Nz * p.nKC * p.ms * (kRawRow / 8);
+    const size_t ad_elems = static_cast<size_t>(p.F) * p.Nz * 4 * p.ms * p.Jp;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_fw), sizeof(float2) * fw_elems)) != CUI_OK) return st;
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_ad), sizeof(float2) * ad_elems)) != CUI_OK) return st;
     if ((st = device_alloc(p, reinterpret_cast<void**>(&p.ws_galign), sizeof(float2) * p.P * p.max_objects)) != CUI_OK)
         return st;
     int blocks = static_cast<int>(std::min<int64_t>((p.tr_vstride + 255) / 256, 152 * 32));
@@ -941,12 +972,13 @@ cui_status tc2_prepare(Plan& p) {
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return check_cuda(e, "band rows");
-    blocks = static_cast<int>(std::min<int64_t>((n_lines * 4 * p.Jp + 255) / 256, 152 * 32));
-    residue_major_kernel<<<blocks, 256>>>(p.p_in, p.p_rm, n_lines, p.Nx, p.Jp);
+    slot_major_fwd_kernel<<<152 * 16, 256>>>(p.p_in, p.f_slot_ptr, p.f_slot_list, p.p_fw, p.F, p.Nz, p.nKC, p.ms, p.Nx, p.P);
     count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "residue-major incident fields");
+    slot_major_adj_kernel<<<152 * 16, 256>>>(p.p_in, p.f_slot_ptr, p.f_slot_list, p.p_ad, p.F, p.Nz, p.ms, p.Jp, p.Nx, p.P);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "slot-major incident fields");
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return check_cuda(e, "line-unit tables");
-    p.tc_bytes += sizeof(uint32_t) * 2 * static_cast<size_t>(p.tr_vstride) + sizeof(float2) * n_lines * 4 * p.Jp +
+    p.tc_bytes += sizeof(uint32_t) * 2 * static_cast<size_t>(p.tr_vstride) + sizeof(float2) * (fw_elems + ad_elems) +
                   sizeof(float2) * p.P * p.max_objects;
     p.tc2 = 1;
     return CUI_OK;
