@@ -1,10 +1,15 @@
 """Benchmark of the GB300 Born operator: forward + adjoint applies per second.
 
-Workload (default ``2d-gradient``): 2D, 512x512 FOV at 76.2 um, 128-element
-linear array, 11 quasi-plane waves (-20..20 deg), 192 frequencies over
-2-6 MHz, time-causal absorption.  One step = one gradient of
-0.5||Phi gamma - u||^2 (forward, residual, adjoint) at a seeded Gaussian
-gamma through the C-ABI (``cui_born_vjp``) -- one forward + adjoint apply.
+Workload (default ``2d-batched``, the batched split-precision configuration):
+2D, 512x512 FOV at 76.2 um, 128-element linear array, 16 random-apodization
+incident waves mixed into 32 receive signals by +-1 weights, 128 frequencies
+over 2.5-5.5 MHz, 64 right-hand-side gamma columns.  One step = one gradient
+of 0.5||Phi gamma - u||^2 (forward, residual, adjoint) for all 64 columns
+through the C-ABI (``cui_born_vjp``) -- 64 forward + adjoint applies.  The
+same plan then times the plain FP32 path on the same inputs, so the line
+carries the split-BF16 / FP32 speed-up and the split-BF16 gradient's error
+against the FP32 one.  ``--workload 2d-gradient`` runs the single-object
+configuration (11 quasi-plane waves, 192 frequencies, time-causal medium).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
@@ -36,12 +41,14 @@ ORACLE_NAME = {"2d-plain": "c0", "2d-gradient": "c1", "2d-batched": "c2", "3d": 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="2d-gradient")
+    ap.add_argument("--workload", default="2d-batched")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--fp32-steps", type=int, default=3,
+                    help="steps of the plain FP32 path timed after the main region (0: skip)")
     ap.add_argument("--precision", choices=["fp32", "bf16x3"], default="bf16x3",
                     help="adjoint contraction: FP32 CUDA cores or split-BF16 tcgen05 tensor cores")
     ap.add_argument("--n-freq", type=int, default=None,
@@ -94,7 +101,8 @@ def roofline_of(args, info, kt, B, clk):
     P = info["n_points"]
     compulsory = info["table_bytes"] + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
     tc = args.precision != "fp32"
-    kernel = {("forward", True): "fwd_tc_kernel", ("adjoint", True): "adj_tc_kernel",
+    # every 2D benchmark workload (4 grid points per pitch, lines a multiple of 8) runs the line-unit kernels
+    kernel = {("forward", True): "fwd_tc2_kernel", ("adjoint", True): "adj_tc2_kernel",
               ("forward", False): "fwd_dense_kernel", ("adjoint", False): "adj_dense_kernel"}[(dom, tc)]
     traffic = launch_traffic(args.workload, kernel, args.n_freq_used)
     hbm = {"compulsory_bytes": compulsory, "achieved_gbs": compulsory / t_launch / 1e9,
@@ -189,9 +197,14 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(workload: str):
+# bounded CPU sample per workload (waves, frequencies, receive mixes): about 10-30 s of host work
+CPU_SAMPLE = {"2d-plain": (1, 8, None), "2d-gradient": (1, 8, None), "2d-batched": (1, 1, 8), "3d": (1, 1, None)}
+
+
+def cpu_baseline(workload: str, n_objects: int):
     from oracle.cpu_baseline import time_sample
-    r = time_sample(ORACLE_NAME[workload], n_waves=1, n_freq=8)
+    nw, nf, nm = CPU_SAMPLE[workload]
+    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm)
     return {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
             "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
 
@@ -211,9 +224,11 @@ def run_reference(args):
         return
     from comp_ui_toolbox_gb300.workloads import workload
     w = workload(args.workload)
-    B = 1
+    B = w.n_objects if args.workload == "2d-batched" else 1
     from oracle.cpu_baseline import time_sample
-    first = time_sample(ORACLE_NAME[args.workload], n_waves=1, n_freq=8, repeats=max(1, args.warmup + args.steps))
+    nw, nf, nm = CPU_SAMPLE[args.workload]
+    first = time_sample(ORACLE_NAME[args.workload], n_waves=nw, n_freq=nf, n_objects=B, n_mixes=nm,
+                        repeats=max(1, min(3, args.warmup + args.steps)))
     t_full = first["seconds_full_apply"]
     value = first["applies_per_s"]
     line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": 0, "steps": args.steps,
@@ -331,9 +346,25 @@ def run_ours(args):
                      "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs},
             "loss": float(loss.sum().item()), "precision": args.precision, "accuracy": accuracy,
             "device_status": op.device_status()}
+    if args.fp32_steps > 0 and args.precision != "fp32":
+        # the plain FP32 path of the same plan on the same inputs: the split-BF16 speed-up
+        op.set_precision("fp32")
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.current_stream())
+        for _ in range(args.fp32_steps):
+            step()
+        e1.record(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1) / args.fp32_steps
+        v32 = world * B / (ms32 / 1e3)
+        line["fp32_comparison"] = {"value": v32, "unit": "applies/s", "ms_per_step": ms32, "steps": args.fp32_steps,
+                                   "speedup_bf16x3_over_fp32": value / v32,
+                                   "rel_l2_grad_bf16x3_vs_fp32": (accuracy or {}).get("rel_l2_grad_vs_fp32")}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline(args.workload)
+            line["cpu_baseline"] = cpu_baseline(args.workload, B)
         except Exception as exc:  # report, never hide
             line["cpu_baseline"] = {"value": None, "error": repr(exc)}
     if rank == 0:

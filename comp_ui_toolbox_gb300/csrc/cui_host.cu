@@ -4,12 +4,15 @@
 // it, runs the operator and converts the FP32 result back to FP64
 // (+scattering/combined_quick_gpu.cu:700-780, :940-1006).  These entry points
 // do the same around the device applies, with pinned staging buffers that
-// the plan allocates on first use and keeps.
+// the plan allocates on first use and keeps.  The FP64 <-> FP32 conversions
+// run on all host cores, and the upload of gamma overlaps the conversion of
+// the measured data.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cui_internal.cuh"
@@ -24,6 +27,8 @@ cui_status ensure_stage(Plan& p) {
     if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
     e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_out), n * sizeof(float2), cudaHostAllocDefault);
     if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_aux), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
     void* v = nullptr;
     for (float2** d : {&p.d_stage_in, &p.d_stage_out, &p.d_stage_aux}) {
         if ((e = cudaMalloc(&v, n * sizeof(float2))) != cudaSuccess) return check_cuda(e, "cudaMalloc");
@@ -37,21 +42,42 @@ cui_status ensure_stage(Plan& p) {
     return CUI_OK;
 }
 
+// fn(lo, hi) over [0, n) split across the host's cores (one thread below 64 Ki elements per core)
+template <class Fn>
+void parallel_for(int64_t n, Fn fn) {
+    const int64_t per = int64_t(1) << 16;
+    const int64_t cores = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(cores, n / per)));
+    if (nt <= 1) {
+        fn(int64_t(0), n);
+        return;
+    }
+    std::vector<std::thread> ts;
+    ts.reserve(nt);
+    for (int t = 0; t < nt; ++t) ts.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+    for (auto& t : ts) t.join();
+}
+
+// column-major FP64 (leading dimension ld) -> packed FP32
 void pack(const cui_complex64* src, int64_t ld, int64_t rows, int B, float2* dst) {
-    for (int b = 0; b < B; ++b)
-        for (int64_t i = 0; i < rows; ++i) {
+    parallel_for(rows * B, [=](int64_t lo, int64_t hi) {
+        for (int64_t k = lo; k < hi; ++k) {
+            const int64_t b = k / rows, i = k - b * rows;
             const cui_complex64 c = src[b * ld + i];
-            dst[b * rows + i] = make_float2(static_cast<float>(c.re), static_cast<float>(c.im));
+            dst[k] = make_float2(static_cast<float>(c.re), static_cast<float>(c.im));
         }
+    });
 }
 
 void unpack(const float2* src, int64_t rows, int B, cui_complex64* dst, int64_t ld) {
-    for (int b = 0; b < B; ++b)
-        for (int64_t i = 0; i < rows; ++i) {
-            const float2 v = src[b * rows + i];
+    parallel_for(rows * B, [=](int64_t lo, int64_t hi) {
+        for (int64_t k = lo; k < hi; ++k) {
+            const int64_t b = k / rows, i = k - b * rows;
+            const float2 v = src[k];
             dst[b * ld + i].re = v.x;
             dst[b * ld + i].im = v.y;
         }
+    });
 }
 
 }  // namespace
@@ -110,9 +136,8 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
     pack(gamma, ld_gamma, p.P, n_objects, p.h_stage_in);
     if ((e = cudaMemcpyAsync(p.d_stage_in, p.h_stage_in, sizeof(float2) * ng, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
         return check_cuda(e, "upload gamma");
-    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return check_cuda(e, "synchronize");
-    pack(u_meas, ld_u, p.n_obs, n_objects, p.h_stage_in);
-    if ((e = cudaMemcpyAsync(p.d_stage_aux, p.h_stage_in, sizeof(float2) * nu, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
+    pack(u_meas, ld_u, p.n_obs, n_objects, p.h_stage_aux);  // overlaps the upload of gamma
+    if ((e = cudaMemcpyAsync(p.d_stage_aux, p.h_stage_aux, sizeof(float2) * nu, cudaMemcpyHostToDevice, 0)) != cudaSuccess)
         return check_cuda(e, "upload u");
     s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0);
     if (s != CUI_OK) return s;

@@ -98,6 +98,7 @@ struct Plan {
     // host-side pinned staging for the FP64 host entry points
     float2* h_stage_in = nullptr;
     float2* h_stage_out = nullptr;
+    float2* h_stage_aux = nullptr;   // second input staging buffer (measured data of the host VJP)
     size_t h_stage_elems = 0;
     float2* d_stage_in = nullptr;   // device copies for the host entry points
     float2* d_stage_out = nullptr;

@@ -67,7 +67,8 @@ void free_plan(Plan& p) {
     p.allocations.clear();
     if (p.h_stage_in) cudaFreeHost(p.h_stage_in);
     if (p.h_stage_out) cudaFreeHost(p.h_stage_out);
-    p.h_stage_in = p.h_stage_out = nullptr;
+    if (p.h_stage_aux) cudaFreeHost(p.h_stage_aux);
+    p.h_stage_in = p.h_stage_out = p.h_stage_aux = nullptr;
 }
 
 inline float2 to_f2(const cui_complex64& c) { return make_float2(static_cast<float>(c.re), static_cast<float>(c.im)); }

@@ -36,7 +36,7 @@ def _sample_config(name: str, n_waves: int, n_freq: int):
     return cfg
 
 
-def _init(name, n_waves, n_freq, seed):
+def _init(name, n_waves, n_freq, seed, n_objects=1):
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     from oracle import configs
@@ -44,7 +44,7 @@ def _init(name, n_waves, n_freq, seed):
     b = configs.build(cfg)
     rng = np.random.default_rng(seed)
     P = cfg.setup.n_points
-    gamma = rng.standard_normal((P, 1))
+    gamma = rng.standard_normal((P, n_objects))
     _STATE.update(b=b, gamma=gamma)
 
 
@@ -65,39 +65,47 @@ def _work(args):
 
 
 def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: int | None = None,
-                repeats: int = 1, seed: int = 0):
+                repeats: int = 1, seed: int = 0, n_objects: int = 1, n_mixes: int | None = None):
     """Seconds per forward+adjoint apply of the full workload, extrapolated from a sample.
 
-    Returns a dict with the sample description, the measured seconds and the
-    extrapolated full-workload applies/s.
+    ``n_mixes`` keeps only the first receive mixes of every wave (work is linear
+    in the mixes when every mix has the same active elements, as in the
+    benchmark workloads).  Returns a dict with the sample description, the
+    measured seconds and the extrapolated full-workload applies/s.
     """
     from oracle import configs
     full = configs.config(name)
     S_full = len(full.waves) * len(full.f)
     S_sample = n_waves * n_freq
-    n_mix = full.setup.n_elements if full.mixing == "identity" else full.n_mixes
+    n_mix_full = full.setup.n_elements if full.mixing == "identity" else full.n_mixes
+    n_mix = min(n_mix_full, n_mixes or n_mix_full)
     procs = processes or os.cpu_count() or 1
     procs = max(1, min(procs, n_mix))
     bounds = np.linspace(0, n_mix, procs + 1).round().astype(int)
     chunks = [(int(bounds[i]), int(bounds[i + 1])) for i in range(procs)]
+    # one BLAS thread per worker: the spawned interpreters read these before importing numpy
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed)) as pool:
+    with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed, n_objects)) as pool:
         pool.map(_work, [(0, 0)] * procs)  # wait until every worker holds its tables
         times = []
         for _ in range(repeats):
             # critical path of the parallel apply: the slowest worker's own compute time
             times.append(max(t for t, _ in pool.map(_work, chunks, chunksize=1)))
     t_sample = min(times)
-    t_full = t_sample * S_full / S_sample
+    t_full = t_sample * (S_full / S_sample) * (n_mix_full / n_mix)
     return {
         "seconds_sample": t_sample,
         "seconds_full_apply": t_full,
-        "applies_per_s": 1.0 / t_full,
+        "applies_per_s": n_objects / t_full,  # object-applies: all columns go through one BLAS call per element
         "cores": procs,
-        "sample": f"{n_waves} of {len(full.waves)} waves x {n_freq} of {len(full.f)} frequencies, full "
+        "sample": f"{n_waves} of {len(full.waves)} waves x {n_freq} of {len(full.f)} frequencies x {n_objects} "
+                  f"gamma columns, full "
                   f"{'x'.join(map(str, full.setup.n_points_axis))} grid, all {full.setup.n_elements} elements; "
                   f"one forward + one adjoint (FP64 numpy/scipy restatement of forward_quick_cpu/adjoint_quick_cpu), "
-                  f"mixes split over {procs} spawn processes; full-workload rate = sample rate x {S_sample}/{S_full}",
+                  f"{n_mix} of {n_mix_full} receive mixes split over {procs} spawn processes; full-workload rate = "
+                  f"sample rate x {S_sample}/{S_full} x {n_mix}/{n_mix_full}",
     }
 
 
