@@ -114,6 +114,8 @@ _SIGNATURES = {
     "cui_born_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
     "cui_born_vjp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
                                C.c_int64, C.c_void_p, C.c_void_p]),
+    "cui_born_lasso": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
+                                 C.c_float, C.c_int32, C.c_void_p, C.c_void_p]),
     "cui_born_combined_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
                                          C.c_int64]),
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
@@ -459,6 +461,53 @@ class OperatorBorn:
                                            B, grad.ctypes.data, self.n_points,
                                            loss.ctypes.data_as(C.POINTER(C.c_double))))
         return (grad[:, 0], loss[0]) if vec else (grad, loss)
+
+    def lasso_(self, gamma_cols, u_cols, lam, step: float, n_iter: int, loss=None, stream=None):
+        """``n_iter`` proximal-gradient LASSO iterations in place (``cui_born_lasso``).
+
+        ``gamma_cols`` (B, n_points) and ``u_cols`` (B, n_observations) are
+        contiguous complex64 device tensors (one object per row), ``lam`` a
+        float32 device tensor of B thresholds, ``loss`` an optional float32
+        device tensor of B values.  Launches only on ``stream`` (default: the
+        current torch stream) and allocates nothing, so it may be captured in a
+        CUDA graph.
+        """
+        import torch
+        B = gamma_cols.shape[0]
+        st = stream if stream is not None else torch.cuda.current_stream(gamma_cols.device).cuda_stream
+        _check(self._lib.cui_born_lasso(self._plan, u_cols.data_ptr(), u_cols.shape[1], B, gamma_cols.data_ptr(),
+                                        gamma_cols.shape[1], lam.data_ptr(), float(step), int(n_iter),
+                                        loss.data_ptr() if loss is not None else None, st))
+
+    def lasso(self, u_meas, lam, step: float, n_iter: int, gamma0=None):
+        """Solve ``min 0.5||Phi gamma - u||^2 + lam ||gamma||_1`` per column by ``n_iter``
+        proximal-gradient steps from ``gamma0`` (zeros by default); returns ``(gamma, loss)``."""
+        import torch
+        uc, vec = self._cols(u_meas)
+        B = uc.shape[0]
+        if gamma0 is None:
+            gc = torch.zeros((B, self.n_points), dtype=torch.complex64, device=uc.device)
+        else:
+            gc, _ = self._cols(gamma0)
+            gc = gc.clone()
+        lam_t = torch.as_tensor(lam, dtype=torch.float32, device=uc.device).reshape(-1).expand(B).contiguous()
+        loss = torch.empty(B, dtype=torch.float32, device=uc.device)
+        self.lasso_(gc, uc, lam_t, step, n_iter, loss)
+        g = gc.t()
+        return (g[:, 0], loss[0]) if vec else (g, loss)
+
+    def norm_estimate(self, n_iter: int = 20, seed: int = 0) -> float:
+        """||Phi||_2^2 by power iteration on Phi^H Phi (device applies)."""
+        import torch
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        x = torch.randn((self.n_points, 1), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
+        x = x / x.norm()
+        lam = 0.0
+        for _ in range(n_iter):
+            y = self.adjoint(self.forward(x))
+            lam = float(y.norm())
+            x = y / lam
+        return lam
 
 
 def _autograd():

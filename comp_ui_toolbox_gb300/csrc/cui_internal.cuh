@@ -163,6 +163,9 @@ cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, floa
                           cudaStream_t st);
 cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg,
                           cudaStream_t st);
+// n_iter proximal-gradient LASSO iterations, gamma updated in place (no allocation, no synchronisation)
+cui_status lasso_device(Plan* p, float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B, float step,
+                        const float* lambda, int n_iter, float* loss, cudaStream_t st);
 cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
                       float2* grad, int64_t ldgr, float* loss, cudaStream_t st);
 

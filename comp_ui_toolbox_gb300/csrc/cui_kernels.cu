@@ -441,6 +441,32 @@ __global__ void reduce_fchunks_kernel(const float2* __restrict__ part, int nfc, 
     }
 }
 
+// Proximal-gradient (ISTA) step fused into the adjoint's final reduction:
+//   v = gamma - step * sum_k part[k],   gamma <- v * max(0, 1 - step*lambda_b / |v|)
+// (complex soft threshold, the proximal map of step*lambda_b*||gamma||_1).  Each
+// element is read and written by one thread, so the update is in place.
+__global__ void ista_reduce_kernel(const float2* __restrict__ part, int nfc, int B, int64_t P, float2* gamma, int64_t ldg,
+                                   float step, const float* __restrict__ lambda) {
+    const int64_t n = static_cast<int64_t>(B) * P;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int k = 0; k < nfc; ++k) {
+            const float2 v = part[k * n + i];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        const int64_t b = i / P, pt = i - b * P;
+        float2 g = gamma[b * ldg + pt];
+        g.x = fmaf(-step, s.x, g.x);
+        g.y = fmaf(-step, s.y, g.y);
+        const float tau = step * lambda[b];
+        const float mag = sqrtf(g.x * g.x + g.y * g.y);
+        const float scale = (mag > tau) ? 1.f - tau / mag : 0.f;
+        gamma[b * ldg + pt] = make_float2(g.x * scale, g.y * scale);
+    }
+}
+
 // r = u_pred - u_meas in place; per-block partial sums of 0.5*|r|^2
 constexpr int kLossBlocks = 128;
 
@@ -612,7 +638,24 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     return cudaGetLastError();
 }
 
-cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st) {
+struct IstaArgs {
+    float step;
+    const float* lambda;  // [B] device
+};
+
+// final reduction of the adjoint's frequency-chunk partials: plain sum into g, or the ISTA update of g
+cudaError_t finish_adjoint(Plan* p, int nfc, int B, float2* g, int64_t ldg, const IstaArgs* ista, cudaStream_t st) {
+    const int64_t m = static_cast<int64_t>(B) * p->P;
+    if (ista)
+        ista_reduce_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg, ista->step, ista->lambda);
+    else
+        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
+                        const IstaArgs* ista = nullptr) {
     UnmixArgs a;
     a.u = u; a.ldu = ldu; a.slot_row_ptr = p->slot_row_ptr; a.slot_rows = p->slot_rows;
     a.row_mix = p->row_mix; a.row_fl = p->row_fl; a.mix_nf = p->mix_nf; a.mix_pref_off = p->mix_pref_off;
@@ -629,10 +672,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         } else if ((e = launch_adj_tc(p, B, st)) != cudaSuccess) {
             return e;
         }
-        const int64_t m = static_cast<int64_t>(B) * p->P;
-        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg);
-        count_launch();
-        return cudaGetLastError();
+        return finish_adjoint(p, nfc, B, g, ldg, ista, st);
     }
     switch (pick_nc(p->max_slots_per_f)) {
         case 1: e = launch_adj<1>(p, B, st); break;
@@ -643,10 +683,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         default: e = launch_adj<16>(p, B, st); break;
     }
     if (e != cudaSuccess) return e;
-    const int64_t m = static_cast<int64_t>(B) * p->P;
-    reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, p->adj_nfc, B, p->P, g, ldg);
-    count_launch();
-    return cudaGetLastError();
+    return finish_adjoint(p, p->adj_nfc, B, g, ldg, ista, st);
 }
 
 }  // namespace
@@ -720,6 +757,26 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
         if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "vjp loss");
     }
     return check_cuda(run_adjoint(p, p->ws_r, p->n_obs, B, grad, ldgr, st), "vjp adjoint");
+}
+
+cui_status lasso_device(Plan* p, float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B, float step,
+                        const float* lambda, int n_iter, float* loss, cudaStream_t st) {
+    const IstaArgs ista{step, lambda};
+    for (int it = 0; it < n_iter; ++it) {
+        cudaError_t e = run_forward(p, gamma, ldg, B, p->ws_r, p->n_obs, st);
+        if (e != cudaSuccess) return check_cuda(e, "lasso forward");
+        residual_kernel<<<dim3(kLossBlocks, B), 256, 0, st>>>(p->ws_r, p->n_obs, um, ldu, p->n_obs, p->ws_loss);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "lasso residual");
+        if (loss != nullptr && it == n_iter - 1) {
+            loss_final_kernel<<<(B + 127) / 128, 128, 0, st>>>(p->ws_loss, kLossBlocks, B, loss);
+            count_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "lasso loss");
+        }
+        if ((e = run_adjoint(p, p->ws_r, p->n_obs, B, gamma, ldg, st, &ista)) != cudaSuccess)
+            return check_cuda(e, "lasso adjoint");
+    }
+    return CUI_OK;
 }
 
 size_t loss_workspace_floats(int max_objects) { return static_cast<size_t>(kLossBlocks) * max_objects; }

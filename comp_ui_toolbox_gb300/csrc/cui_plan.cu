@@ -524,6 +524,20 @@ cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t
                            ld_grad, loss, static_cast<cudaStream_t>(stream));
 }
 
+cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int64_t ld_u, int32_t n_objects,
+                          cui_complex32* gamma, int64_t ld_gamma, const float* lambda, float step, int32_t n_iter,
+                          float* loss, void* stream) {
+    cui_status s = cui::check_apply(plan, gamma, ld_gamma, plan ? plan->p.P : 0, n_objects, gamma, ld_gamma,
+                                    plan ? plan->p.P : 0);
+    if (s != CUI_OK) return s;
+    if (!u_meas || ld_u < plan->p.n_obs) return set_error(CUI_ERR_INVALID_ARG, "invalid u_meas");
+    if (!lambda) return set_error(CUI_ERR_INVALID_ARG, "lambda is NULL");
+    if (n_iter < 0 || !(step > 0.f)) return set_error(CUI_ERR_INVALID_ARG, "n_iter must be >= 0 and step > 0");
+    cudaSetDevice(plan->p.device);
+    return cui::lasso_device(&plan->p, reinterpret_cast<float2*>(gamma), ld_gamma, reinterpret_cast<const float2*>(u_meas),
+                             ld_u, n_objects, step, lambda, n_iter, loss, static_cast<cudaStream_t>(stream));
+}
+
 cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable) {
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     plan->p.timing = enable != 0;

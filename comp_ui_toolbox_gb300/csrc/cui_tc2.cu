@@ -177,9 +177,11 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
     extern __shared__ __align__(1024) unsigned char smem[];
     const FwdLayout<NT> L(a.ms, a.Bt, a.RBW);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int grp = blockIdx.x, f = blockIdx.y;
+    // the column tile varies fastest: the tiles of one line group and frequency run together and
+    // share the table rows and incident-field segments through L2
+    const int grp = blockIdx.y, f = blockIdx.z;
     const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
-    const int b0 = blockIdx.z * a.Bt;
+    const int b0 = blockIdx.x * a.Bt;
     const int line0 = grp * a.lines_per_group, line1 = min(line0 + a.lines_per_group, a.n_lines);
     if (ns == 0 || b0 >= a.B || line0 >= line1) return;  // uniform over the block
     // a block of an earlier launch gave up (status not yet read): skip the work, keep the error
@@ -493,8 +495,10 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     extern __shared__ __align__(1024) unsigned char smem[];
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int z = blockIdx.x, fc = blockIdx.y;
-    const int b0 = blockIdx.z * a.Bt;
+    // the column tile varies fastest: the tiles of one line and frequency chunk run together and
+    // share the table rows and incident fields through L2
+    const int z = blockIdx.y, fc = blockIdx.z;
+    const int b0 = blockIdx.x * a.Bt;
     if (b0 >= a.B) return;  // uniform
     if (__syncthreads_or(tid == 0 && (*reinterpret_cast<volatile int*>(a.status) & 6) != 0)) return;
     const int f_lo = fc * a.fchunk, f_hi = min(f_lo + a.fchunk, a.F);
@@ -877,7 +881,7 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
                                   static_cast<int>(smem))) != cudaSuccess)
         return e;
     if ((e = timing_begin(p, 0, st)) != cudaSuccess) return e;
-    fwd_tc2_kernel<NT><<<dim3(groups, p->F, t.tiles), kThreads2, smem, st>>>(a);
+    fwd_tc2_kernel<NT><<<dim3(t.tiles, groups, p->F), kThreads2, smem, st>>>(a);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *groups_out = groups;
@@ -901,7 +905,7 @@ cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nf
                                          static_cast<int>(L.total));
     if (e != cudaSuccess) return e;
     if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
-    adj_tc2_kernel<NT><<<dim3(p->Nz, nfc, t.tiles), kThreads2, L.total, st>>>(a);
+    adj_tc2_kernel<NT><<<dim3(t.tiles, p->Nz, nfc), kThreads2, L.total, st>>>(a);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *nfc_out = nfc;

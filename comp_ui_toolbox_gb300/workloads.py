@@ -14,7 +14,12 @@ synthetic setups stand in with the stated shapes, sizes and distributions:
   random apodization in [-1, 1] and random delays in [0, 1] us, 32 receive
   mixes with random +-1 weights, 64 gamma columns at 3% density;
 * ``3d``: 32x32 matrix array at 0.3 mm, 5 quasi-plane waves -10..10 deg
-  azimuth, 64 frequencies, 128^3 FOV at 0.1 mm from 5 mm, absorbing, gamma 1%.
+  azimuth, 64 frequencies, 128^3 FOV at 0.1 mm from 5 mm, absorbing, gamma 1%;
+* ``2d-lasso`` (:func:`lasso_batch`): independent 2D problems of seeded sizes
+  (FOV side in {128, 192, 256, 384, 512} at 76.2 um, 1-16 quasi-plane waves
+  over -20..20 deg, 32-256 frequencies over 2.5-5.5 MHz, 64 or 128 elements at
+  0.3048 mm pitch, lossless), gamma_true 2%, data with 25 dB noise, each
+  solved by 50 proximal-gradient LASSO iterations.
 
 The wave synthesis restates the reference's delay laws: quasi-plane-wave
 delays ``<x_e, e_theta>/c`` shifted to zero minimum
@@ -150,6 +155,33 @@ def workload(name: str) -> Workload:
                         (1, 1), TISSUE, np.linspace(2.5e6, 5.5e6, 64),
                         [("qpw", (float(a), 0.0)) for a in (-10, -5, 0, 5, 10)], density=0.01, seed=1003)
     raise KeyError(name)
+
+
+def lasso_problem(i: int, seed: int = 4000) -> Workload:
+    """Problem ``i`` of the seeded uneven batch (sizes drawn independently per problem)."""
+    rng = np.random.default_rng(seed + i)
+    side = int(rng.choice([128, 192, 256, 384, 512]))
+    n_waves = int(rng.integers(1, 17))
+    n_f = int(rng.integers(32, 257))
+    n_el = int(rng.choice([64, 128]))
+    angles = np.linspace(-20.0, 20.0, n_waves) if n_waves > 1 else np.array([0.0])
+    return Workload(f"2d-lasso[{i}]", (side, side), (DX_2D, DX_2D), 5e-3, (n_el,), (PITCH_L14,), (WIDTH_L14,), (1,),
+                    LOSSLESS, np.linspace(2.5e6, 5.5e6, n_f), [("qpw", (float(a),)) for a in angles],
+                    density=0.02, seed=seed + 1000 + i)
+
+
+def lasso_batch(n_problems: int, seed: int = 4000) -> list:
+    """The first ``n_problems`` problems of the seeded uneven batch."""
+    return [lasso_problem(i, seed) for i in range(n_problems)]
+
+
+def plan_bytes_estimate(w: Workload, tensor_cores: bool = True) -> int:
+    """Device bytes a plan of ``w`` holds (tables, incident fields, their split-BF16 copies)."""
+    Nx, Nz = w.n_points_axis[0], w.n_points_axis[-1]
+    F, W, E = len(w.f), len(w.waves), w.n_elements
+    table = F * Nz * (Nx + (E - 1) * 4) * 8
+    incident = W * F * w.n_points * 8
+    return int(table * (2 if tensor_cores else 1) + incident * (3.2 if tensor_cores else 1))
 
 
 NAMES = ("2d-plain", "2d-gradient", "2d-batched", "3d")

@@ -212,6 +212,20 @@ cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t
                         const cui_complex32* u_meas, int64_t ld_u, int32_t n_objects,
                         cui_complex32* grad, int64_t ld_grad, float* loss, void* stream);
 
+/* Proximal-gradient (ISTA) LASSO iterations of the data-fidelity term above,
+ * the solver loop the reference drives through combined_scalar
+ * (+scattering/operator.m:717, lq_minimization :601-790):
+ *   r = Phi*gamma - u_meas;  gamma <- S(gamma - step * Phi^H r, step * lambda[b])
+ * with the complex soft threshold S(v, t) = v * max(0, 1 - t/|v|), n_iter times,
+ * gamma (device, n_points x n_objects) updated in place.  `lambda` is a device
+ * array of n_objects floats; `step` should not exceed 1/||Phi||^2.  `loss`
+ * (device, may be NULL) receives 0.5*||r||^2 of the last iteration's iterate.
+ * Every launch goes to `stream` and nothing is allocated or synchronised, so a
+ * caller may capture the iterations of one or many plans into a CUDA graph. */
+cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int64_t ld_u, int32_t n_objects,
+                          cui_complex32* gamma, int64_t ld_gamma, const float* lambda, float step, int32_t n_iter,
+                          float* loss, void* stream);
+
 /* ---- host applies (FP64, MEX semantics) ----------------------------------
  * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
  * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).

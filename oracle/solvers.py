@@ -1,0 +1,63 @@
+"""FP64 restatement of the solver loop that drives the Born operator (test infrastructure).
+
+TEST INFRASTRUCTURE ONLY: used by ``tests/`` as the checker of the library's
+device LASSO iterations (``cui_born_lasso``); nothing in the product imports it.
+
+The reference solves its sparse-recovery problems through
+``operator.lq_minimization`` (``+scattering/operator.m:601-790``), which wraps
+the operator as ``op_A(x, mode) = combined_scalar(op, mode, x)`` (``:717``) and
+hands it to an algorithm object (``:723-726``): SPGL1 (``+regularization/
++algorithms/+convex/spgl1.m:154``, the external spgl1-1.8 package, not vendored)
+or OMP/CoSaMP.  Every such iteration is a forward apply, a residual and an
+adjoint apply -- the gradient of 0.5||Phi gamma - u||^2.  The uneven-batch
+workload runs the plainest member of that family, proximal-gradient LASSO
+(ISTA):
+
+    gamma <- S(gamma - t Phi^H (Phi gamma - u), t lambda),  S(v, s) = v max(0, 1 - s/|v|)
+
+which is what :func:`lasso_ista` restates with the oracle's FP64 operator.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .born_oracle import OperatorTables, adjoint_quick_cpu, forward_quick_cpu
+
+
+def soft_threshold(v: np.ndarray, s) -> np.ndarray:
+    """Complex soft threshold ``v * max(0, 1 - s/|v|)`` (proximal map of ``s * ||v||_1``)."""
+    mag = np.abs(v)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        scale = np.where(mag > s, 1.0 - s / np.where(mag > 0, mag, 1.0), 0.0)
+    return v * scale
+
+
+def lasso_ista(op: OperatorTables, u: np.ndarray, lam, step: float, n_iter: int, gamma0=None):
+    """``n_iter`` ISTA iterations per column of ``u``; returns ``(gamma, loss)`` where ``loss``
+    is ``0.5||Phi gamma_k - u||^2`` of the last iteration's input iterate (per column)."""
+    u = np.asarray(u, dtype=np.complex128)
+    u2 = u[:, None] if u.ndim == 1 else u
+    B = u2.shape[1]
+    P = op.setup.n_points
+    g = np.zeros((P, B), dtype=np.complex128) if gamma0 is None else np.array(gamma0, dtype=np.complex128).reshape(P, B)
+    lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (B,))
+    loss = np.zeros(B)
+    for _ in range(n_iter):
+        r = forward_quick_cpu(op, g) - u2
+        loss = 0.5 * np.sum(np.abs(r) ** 2, axis=0)
+        g = soft_threshold(g - step * adjoint_quick_cpu(op, r), step * lam[None, :])
+    return g, loss
+
+
+def operator_norm2(op: OperatorTables, n_iter: int = 30, seed: int = 0) -> float:
+    """||Phi||_2^2 by power iteration on Phi^H Phi (FP64)."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((op.setup.n_points, 1)) + 0j
+    x /= np.linalg.norm(x)
+    lam = 0.0
+    for _ in range(n_iter):
+        y = adjoint_quick_cpu(op, forward_quick_cpu(op, x))
+        lam = float(np.linalg.norm(y))
+        x = y / lam
+    return lam
