@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--fp32-steps", type=int, default=3,
                     help="steps of the plain FP32 path timed after the main region (0: skip)")
-    ap.add_argument("--precision", choices=["fp32", "bf16x3"], default="bf16x3",
+    ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default="bf16x3",
                     help="adjoint contraction: FP32 CUDA cores or split-BF16 tcgen05 tensor cores")
     ap.add_argument("--lasso-problems", type=int, default=16,
                     help="2d-lasso: how many of the 256 seeded problems go into the graph (device memory bound)")
@@ -322,13 +322,15 @@ def run_ours(args):
 
     # end to end through the host (FP64) entry point: copies inside the timed region
     e2e_steps = args.e2e_steps or max(1, min(args.steps, 5))
-    g_host = gamma.cpu().numpy().astype(np.complex128)
-    u_host = u_meas.cpu().numpy().astype(np.complex128)
-    op.vjp(g_host, u_host)
+    # host buffers as a MATLAB caller holds them: column-major complex128, output reused
+    g_host = np.asfortranarray(gamma.cpu().numpy().astype(np.complex128))
+    u_host = np.asfortranarray(u_meas.cpu().numpy().astype(np.complex128))
+    grad_out = np.empty_like(g_host, order="F")
+    op.vjp(g_host, u_host, out=grad_out)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        grad_h, loss_h = op.vjp(g_host, u_host)
+        grad_h, loss_h = op.vjp(g_host, u_host, out=grad_out)
     t_e2e = time.perf_counter() - t0
     e2e = {"value": e2e_steps * B / t_e2e, "unit": "applies/s",
            "h2d_bytes_per_step": 8 * (P + N) * B, "d2h_bytes_per_step": 8 * P * B + 4 * B,
@@ -419,9 +421,13 @@ def run_lasso(args):
     t_build = time.perf_counter() - t0
     streams = [torch.cuda.Stream() for _ in range(4)]
 
+    tuned = []
+    if args.precision == "auto":  # per-plan autotuner: the faster path for each problem
+        tuned = [op.autotune(1) for op in ops]
+
     def capture(precision):
-        for op in ops:
-            op.set_precision(precision)
+        for op, tu in zip(ops, tuned or [None] * len(ops)):
+            op.set_precision(tu["precision"] if (precision == "auto" and tu) else precision)
         for op, g, u, lam, st in zip(ops, gs, us, lams, steps):  # first use outside the capture
             op.lasso_(g, u, lam, st, 1)
         torch.cuda.synchronize()
@@ -469,7 +475,8 @@ def run_lasso(args):
     line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32" if precision == "fp32" else "bf16x3 (split-BF16 operands, f32 accumulate)",
+            "dtype": {"fp32": "f32", "auto": "per problem: f32 or bf16x3 (autotuned)"}.get(
+                precision, "bf16x3 (split-BF16 operands, f32 accumulate)"),
             "data": "synthetic (seeded)",
             "config": {"workload": f"2d-lasso: first {len(ops)} of the 256 seeded uneven problems (FOV side "
                                    f"128-512, 1-16 waves, 32-256 frequencies, 64/128 elements), {n_it} "
@@ -482,6 +489,7 @@ def run_lasso(args):
             "gpu_launches": n_launch_graph * args.steps,
             "graph": {"kernel_nodes_captured": n_launch_graph, "replays": args.steps},
             "clocks": clocks.summary(), "plan": {"build_s": t_build}, "precision": precision,
+            "autotune": tuned or None,
             "objective_after": objective}
     # end to end: host FP64 data in, FP64 solution out, around one graph replay
     u_host = [u.cpu().numpy().astype(np.complex128) for u in us]
@@ -506,7 +514,7 @@ def run_lasso(args):
         rel = max(float((g.cpu() - gt.cpu()).norm() / max(gt.cpu().norm(), 1e-30)) for g, gt in zip(gs, g_tc))
         line["fp32_comparison"] = {"value": world * len(ops) * n_it / (ms32 / 1e3), "unit": "applies/s",
                                    "ms_per_step": ms32, "steps": args.fp32_steps,
-                                   "speedup_bf16x3_over_fp32": ms32 / ms,
+                                   f"speedup_{precision}_over_fp32": ms32 / ms,
                                    "max_rel_l2_solution_bf16x3_vs_fp32": rel}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -121,6 +121,7 @@ _SIGNATURES = {
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
     "cui_born_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "cui_born_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
     "cui_born_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
     "cui_born_timing_read": (C.c_int, [C.c_void_p, C.POINTER(BornTiming)]),
@@ -354,6 +355,16 @@ class OperatorBorn:
         _check(self._lib.cui_born_set_precision(self._plan, {"fp32": 0, "bf16x3": 1}[precision]))
         self.precision = precision
 
+    def autotune(self, n_objects: int = 1) -> dict:
+        """Keep the faster of the FP32 and split-BF16 paths for ``n_objects`` columns
+        (``cui_born_autotune``); returns the choice and both times."""
+        import torch
+        choice = C.c_int32(0)
+        ms = (C.c_double * 2)()
+        st = torch.cuda.current_stream().cuda_stream
+        _check(self._lib.cui_born_autotune(self._plan, int(n_objects), C.byref(choice), ms, st))
+        return {"precision": "bf16x3" if choice.value == 1 else "fp32", "ms_fp32": ms[0], "ms_bf16x3": ms[1]}
+
     def device_status(self) -> int:
         """Read and clear the device status word (raises CuiError on a timed-out wait)."""
         s = C.c_int32()
@@ -435,8 +446,14 @@ class OperatorBorn:
             return self.adjoint(x)
         raise CuiError(1, "mode must be 0, 1 or 2")
 
-    def vjp(self, gamma, u_meas):
-        """Gradient and value of ``0.5*||Phi gamma - u||^2`` per column: ``(grad, loss)``."""
+    def vjp(self, gamma, u_meas, out=None):
+        """Gradient and value of ``0.5*||Phi gamma - u||^2`` per column: ``(grad, loss)``.
+
+        Host (numpy) inputs follow the MEX semantics; column-major complex128
+        arrays (MATLAB's layout) pass through without a copy, and ``out`` (a
+        column-major complex128 array of gamma's shape) receives the gradient
+        without a new allocation.
+        """
         if self._is_torch(gamma):
             import torch
             gc, vec = self._cols(gamma)
@@ -455,7 +472,12 @@ class OperatorBorn:
         g2 = _c128_f(g[:, None] if vec else g)
         u2 = _c128_f(np.asarray(u_meas)[:, None] if vec else u_meas)
         B = g2.shape[1]
-        grad = np.zeros((self.n_points, B), dtype=np.complex128, order="F")
+        if out is not None:
+            grad = out[:, None] if out.ndim == 1 else out
+            if grad.dtype != np.complex128 or not grad.flags.f_contiguous or grad.shape != (self.n_points, B):
+                raise CuiError(1, "out must be a column-major complex128 array of gamma's shape")
+        else:
+            grad = np.empty((self.n_points, B), dtype=np.complex128, order="F")
         loss = np.zeros(B, dtype=np.float64)
         _check(self._lib.cui_born_vjp_host(self._plan, g2.ctypes.data, g2.shape[0], u2.ctypes.data, u2.shape[0],
                                            B, grad.ctypes.data, self.n_points,

@@ -249,6 +249,16 @@ typedef enum { CUI_PRECISION_FP32 = 0, CUI_PRECISION_BF16X3 = 1 } cui_precision;
 
 cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precision);
 
+/* Autotuner (no counterpart in the reference, whose MEX has one path): times one
+ * forward + adjoint apply of each path this plan can run for `n_objects`
+ * columns -- the FP32 CUDA-core kernels and, for 2D setups, the split-BF16
+ * tensor-core kernels -- on `stream` and keeps the faster (as
+ * cui_born_set_precision would).  Both paths meet the operator's accuracy bound.
+ * Allocates and frees scratch buffers and synchronises: call it at set-up,
+ * before any stream capture.  `precision` (may be NULL) receives the choice,
+ * `ms` (may be NULL) the two times in ms (FP32, BF16X3; -1 when not run). */
+cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, int32_t* precision, double* ms, void* stream);
+
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Device time of the two contraction kernels, from CUDA events recorded on
  * the launching stream around each launch while timing is enabled. */

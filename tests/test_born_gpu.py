@@ -339,3 +339,19 @@ def test_bf16x3_full_lines_match_fp32(wname, n_freq, n_obj):
         assert rel_l2(u16[:, b], u32[:, b]) <= TOL
         assert rel_l2(a16[:, b], a32[:, b]) <= TOL
     op.close()
+
+
+@pytest.mark.parametrize("name", ["c1", "c3"])
+def test_autotune_keeps_a_path_that_matches_oracle(name):
+    """cui_born_autotune times the FP32 and (2D) split-BF16 paths, keeps the faster,
+    and the plan's outputs stay within the operator's bound."""
+    b = built(name)
+    op = make_operator(b, "lateral", max_objects=1)
+    res = op.autotune(1)
+    assert res["ms_fp32"] > 0
+    assert (res["ms_bf16x3"] > 0) == (name != "c3")  # the 3D setup has no tensor-core path
+    assert res["precision"] in ("fp32", "bf16x3")
+    gamma = configs.make_gamma(b.cfg, complex_values=True)
+    u = op.forward(dev(gamma)).cpu().numpy()
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
+    assert op.device_status() == 0
