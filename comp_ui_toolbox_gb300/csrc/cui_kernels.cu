@@ -528,6 +528,22 @@ int pick_nc(int slots) {
 constexpr int fwd_ke(int nc) { return nc >= 16 ? 2 : 4; }
 constexpr int adj_kj(int nc) { return nc >= 12 ? 2 : 4; }
 
+// Register-window length per lane: the native length k0 when the warp's lanes
+// (32 x k per group) are mostly busy over n items (elements for the forward,
+// points of a residue for the adjoint), else a shorter one.  The 2D arrays
+// (128 elements, 128 points per residue) keep k0; the 3D matrix array's rows
+// (32 elements, 43 points per residue) would leave 3 of 4 lanes idle with k0 = 4.
+int pick_window(int n, int k0) {
+    auto util = [n](int k) {
+        const int per = 32 * k;
+        return static_cast<double>(n) / (static_cast<double>((n + per - 1) / per) * per);
+    };
+    int best = k0;
+    for (int k : {2, 1})
+        if (k < k0 && util(k) > util(best) + 1e-9) best = k;
+    return best;
+}
+
 struct FwdShape { int n_eg, nseg, Js, ntask, threads; };
 struct AdjShape { int n_jg, nseg_e, Es, ntask, threads; };
 
@@ -555,9 +571,8 @@ AdjShape adj_shape(const Plan* p, int kj) {
     return s;
 }
 
-template <int NC>
-cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
-    constexpr int KE = fwd_ke(NC);
+template <int NC, int KE>
+cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
     const FwdShape sh = fwd_shape(p, KE);
     FwdArgs a;
     a.g = geom_of(p);
@@ -579,9 +594,8 @@ cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, c
     return timing_end(const_cast<Plan*>(p), st);
 }
 
-template <int NC>
-cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
-    constexpr int KJ = adj_kj(NC);
+template <int NC, int KJ>
+cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
     const AdjShape sh = adj_shape(p, KJ);
     AdjArgs a;
     a.g = geom_of(p);
@@ -600,6 +614,26 @@ cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return timing_end(const_cast<Plan*>(p), st);
+}
+
+template <int NC>
+cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
+    constexpr int K0 = fwd_ke(NC);
+    switch (pick_window(p->Ex, K0)) {
+        case 1: return launch_fwd_k<NC, 1>(p, gamma, ldg, B, st);
+        case 2: return launch_fwd_k<NC, (K0 > 2 ? 2 : K0)>(p, gamma, ldg, B, st);
+        default: return launch_fwd_k<NC, K0>(p, gamma, ldg, B, st);
+    }
+}
+
+template <int NC>
+cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
+    constexpr int K0 = adj_kj(NC);
+    switch (pick_window(p->Nj_max, K0)) {
+        case 1: return launch_adj_k<NC, 1>(p, B, st);
+        case 2: return launch_adj_k<NC, (K0 > 2 ? 2 : K0)>(p, B, st);
+        default: return launch_adj_k<NC, K0>(p, B, st);
+    }
 }
 
 int grid_1d(int64_t n, int threads) {
@@ -690,8 +724,8 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
 
 bool launch_shapes_ok(const Plan* p, std::string* why) {
     const int nc = pick_nc(p->max_slots_per_f);
-    const FwdShape f = fwd_shape(p, nc >= 16 ? 2 : 4);
-    const AdjShape a = adj_shape(p, nc >= 12 ? 2 : 4);
+    const FwdShape f = fwd_shape(p, pick_window(p->Ex, nc >= 16 ? 2 : 4));
+    const AdjShape a = adj_shape(p, pick_window(p->Nj_max, nc >= 12 ? 2 : 4));
     if (f.threads > 512 || a.threads > 512) {
         *why = "launch shape exceeds 512 threads (too many points per pitch or elements for this build)";
         return false;
