@@ -107,14 +107,20 @@ __global__ void row_kernel(const float2* __restrict__ table, uint32_t* __restric
     }
 }
 
-// Column tiles: Bt == 1 -> column c is slot c of the frequency (ns <= NT), one
-// object; Bt == 2 -> the column halves hold objects b0 and b0+1, column
-// c = h*NT/2 + slot (ns <= NT/2).  Returns the slot index (-1: unused) and object.
+// Column tiles of Bt objects (1, 2 or 4): the tile's NT columns split into Bt
+// equal parts, part k holding object b0 + k with column c = k*NT/Bt + slot
+// (ns <= NT/Bt).  Returns the slot index (-1: unused) and object.
+template <int NT>
+__device__ __forceinline__ int cols_per_object(int Bt) {
+    return Bt == 4 ? NT / 4 : (Bt == 2 ? NT / 2 : NT);
+}
+
 template <int NT>
 __device__ __forceinline__ void column(int c, int ns, int s0, int b0, int Bt, int B, const int* __restrict__ f_slot_list,
                                        int& slot, int& b) {
-    const int bl = (Bt == 2 && c >= NT / 2) ? 1 : 0;
-    const int sl = c - bl * (NT / 2);
+    const int per = cols_per_object<NT>(Bt);
+    const int bl = c / per;
+    const int sl = c - bl * per;
     b = b0 + bl;
     slot = (sl < ns && b < B) ? __ldg(f_slot_list + s0 + sl) : -1;
 }
@@ -148,7 +154,7 @@ struct Fwd2Args {
 
 template <int NT>
 struct FwdCfg {
-    static constexpr int NS = NT >= 32 ? 3 : 4;  // B stages
+    static constexpr int NS = NT >= 64 ? 2 : (NT >= 32 ? 3 : 4);  // B stages
     static constexpr int NR = 4;                 // raw stages
     static constexpr int STB = NT * 1024;        // 4NT rows x 64 points x 4 B
     static constexpr int SBO = 2048;             // 8-row groups: 16 K groups x 128 B
@@ -330,7 +336,8 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             const int ib = warp + 8 * it, cb = ib % (NT / 8), gb = ib / (NT / 8);
             cc[it] = 8 * cb + (lane & 7);
             g4[it] = 4 * gb + (lane >> 3);
-            const int bl = (a.Bt == 2 && cc[it] >= NT / 2) ? 1 : 0, sl = cc[it] - bl * (NT / 2);
+            const int per = cols_per_object<NT>(a.Bt);
+            const int bl = cc[it] / per, sl = cc[it] - bl * per;
             const bool valid = sl < ns && bl < nb;
             prow[it] = valid ? sl * kRawRow + 32 * g4[it] : -1;
             grow[it] = valid ? a.ms * kRawRow + bl * 512 + 32 * g4[it] : -1;
@@ -851,6 +858,18 @@ Tile2 tile2(const Plan* p, int B) {
     return t;
 }
 
+// forward tiles: 64 columns (4 objects x up to 16 waves, N = 256 per MMA) when the batch fills them,
+// so that each staged table row feeds twice the columns; otherwise the adjoint's tiles
+Tile2 tile_fwd(const Plan* p, int B) {
+    const int ms = std::max(1, p->max_slots_per_f);
+    if (B >= 4 && ms >= 12 && ms <= 16) {
+        Tile2 t;
+        t.NT = 64, t.Bt = 4, t.tiles = (B + 3) / 4;
+        return t;
+    }
+    return tile2(p, B);
+}
+
 template <int NT>
 cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const Tile2& t, cudaStream_t st,
                         int* groups_out) {
@@ -921,7 +940,9 @@ size_t tc2_smem_need(const Plan* p, int Epad, int RowW) {
     const int ms = std::max(1, p->max_slots_per_f);
     const int Jp = ((p->Nx + 3) / 4 + 1) / 2 * 2;
     size_t need = 0;
-    for (int B = 1; B <= std::min(p->max_objects, 2); ++B) {
+    for (int B = 1; B <= std::min(p->max_objects, 4); ++B) {
+        const Tile2 tf = tile_fwd(p, B);
+        if (tf.NT == 64) need = std::max(need, FwdLayout<64>(ms, tf.Bt, rbw).total);
         const Tile2 t = tile2(p, B);
         if (t.NT == 16)
             need = std::max({need, FwdLayout<16>(ms, t.Bt, rbw).total, AdjLayout<16>(Epad, rbw, ms, Jp, p->F).total});
@@ -989,7 +1010,8 @@ cui_status tc2_prepare(Plan& p) {
 }
 
 cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* groups) {
-    const Tile2 t = tile2(p, B);
+    const Tile2 t = tile_fwd(p, B);
+    if (t.NT == 64) return launch_fwd2<64>(p, gamma, ldg, B, t, st, groups);
     return t.NT == 16 ? launch_fwd2<16>(p, gamma, ldg, B, t, st, groups) : launch_fwd2<32>(p, gamma, ldg, B, t, st, groups);
 }
 
