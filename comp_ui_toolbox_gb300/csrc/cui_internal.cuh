@@ -132,6 +132,7 @@ struct Plan {
     int nKC = 0;                     // 64-point segments per grid line
     int ms = 0;                      // slot rows per frequency in both layouts (most slots of any frequency)
     float2* ws_galign = nullptr;     // [max_objects][P] aligned copy of a misaligned gamma (forward)
+    uint32_t* ws_vs = nullptr;       // split-BF16 V tiles of the adjoint [F][tiles][tile bytes / 4]
     int* ws_status = nullptr;        // device status word (bounded waits that gave up)
 
     // per-kernel timing (diagnostics): event pairs around contraction launches

@@ -448,22 +448,64 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
 //   Z[j][c] = sum_e' conj(T[r + 4(j + e')]) V[e'][c]
 //   gamma_hat[b_c](x) += conj(p_in[slot_c](x)) Z[j][c]
 // A = spread chunks of residue r (M = 128 point rows j, K = elements e'),
-// B = V columns (N = 4NT stacked rows), loaded once per frequency.
-// B1 = (V_re, V_im) gives Re(conj(T) V); B2 = rot(B1) = (-V_im, V_re) gives -Im.
-// The epilogue reads the incident fields of the unit from a residue-major copy
-// (p_ad[f][z][r][slot of f][j]) that the bulk-copy warp brings in, one copy per unit, and
-// keeps gamma_hat of its 4 points in registers for the whole frequency chunk.
+// expanded by the producers from the table row the bulk-copy warp brings;
+// B = the V columns of the tile, split to bf16 hi/lo once per apply by
+// vsplit_kernel straight into the shared-memory operand layout, so one bulk
+// copy per frequency stages it.  B1 = (V_re, V_im) gives Re(conj(T) V),
+// B2 = rot(B1) = (-V_im, V_re) gives -Im.  The epilogue reads the incident
+// fields of the unit from the slot-major residue copy (p_ad[f][z][r][slot of
+// f][j], one copy per unit) and keeps gamma_hat of its points in registers for
+// the whole frequency chunk.  A block covers L grid lines (2 with 64-column
+// tiles, whose single 128 KB B buffer is then reloaded once per 8 units).
 // ---------------------------------------------------------------------------
+
+// V tiles in the B-operand layout: vs[f][tile][4NT rows x 2Epad bf16], rows
+// [B1 hi | B2 hi | B1 lo | B2 lo], K-major core matrices (8 rows x 16 B), 8-row
+// groups 32*Epad bytes apart -- byte-identical to what a block would stage.
+template <int NT>
+__global__ void vsplit_kernel(const float2* __restrict__ V, const int* __restrict__ f_slot_ptr,
+                              const int* __restrict__ f_slot_list, uint32_t* __restrict__ vs, int F, int tiles, int Bt,
+                              int B, int E, int Ex, int Epad) {
+    const int64_t tile_words = 4ll * NT * Epad;  // 32-bit words of one tile: 4NT rows x 2Epad bf16
+    const int64_t n = static_cast<int64_t>(F) * tiles * NT * (Epad / 4);
+    const int SBOB = 32 * Epad;
+    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
+         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t t = idx;
+        const int g = static_cast<int>(t % (Epad / 4)); t /= Epad / 4;
+        const int c = static_cast<int>(t % NT); t /= NT;
+        const int tile = static_cast<int>(t % tiles);
+        const int f = static_cast<int>(t / tiles);
+        const int s0 = f_slot_ptr[f], ns = f_slot_ptr[f + 1] - s0;
+        int sl, b;
+        column<NT>(c, ns, s0, tile * Bt, Bt, B, f_slot_list, sl, b);
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int e = Ex - 1 - (4 * g + k);
+            float2 v = make_float2(0.f, 0.f);
+            if (sl >= 0 && e >= 0) v = V[(static_cast<int64_t>(sl) * B + b) * E + e];
+            split(v.x, v.y, hw[k], lw[k]);
+        }
+        uint4* base = reinterpret_cast<uint4*>(vs + (static_cast<int64_t>(f) * tiles + tile) * tile_words);
+        base[b_off(c, g, SBOB) / 16] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        base[b_off(NT + c, g, SBOB) / 16] = make_uint4(rot(hw[0]), rot(hw[1]), rot(hw[2]), rot(hw[3]));
+        base[b_off(2 * NT + c, g, SBOB) / 16] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        base[b_off(3 * NT + c, g, SBOB) / 16] = make_uint4(rot(lw[0]), rot(lw[1]), rot(lw[2]), rot(lw[3]));
+    }
+}
+
 struct Adj2Args {
     const uint32_t* tr;
     int64_t tr_vstride;
     int RowW, RBW;
     const float2* p_ad;  // [F][Nz][4][ms][Jp]
     int Jp;
-    const float2* V;     // [S][B][E]
+    const uint32_t* vs;  // [F][tiles][tile bytes / 4] split V tiles (vsplit_kernel)
+    int tiles;
     const int* f_slot_ptr;
     const int* f_slot_list;
-    int Nx, Nz, Ex, E, Epad, B, Bt, F, fchunk, ms;
+    int Nx, Nz, Ex, E, Epad, B, Bt, F, fchunk, ms, L;
     int64_t P;
     float2* part;        // [nfc][B][P]
     int* status;
@@ -471,10 +513,12 @@ struct Adj2Args {
 
 template <int NT>
 struct AdjCfg {
-    static constexpr int NA = 3;               // spread-chunk stages
-    static constexpr int NP = 3;               // incident-field stages
-    static constexpr uint32_t TCOLS = 8 * NT;  // 2 accumulators x 4NT columns
-    static constexpr int LAG = 2;              // the epilogue trails the spreading by 2 units
+    static constexpr int NB = NT >= 64 ? 1 : 2;  // V tile buffers (128 KB each at 64 columns)
+    static constexpr int NA = 3;                 // spread-chunk stages
+    static constexpr int NP = 3;                 // incident-field stages
+    static constexpr uint32_t TCOLS = 8 * NT;    // 2 accumulators x 4NT columns
+    static constexpr int LAG = 2;                // the epilogue trails the spreading by 2 units
+    static constexpr int MAXL = 2;               // grid lines per block
 };
 
 template <int NT>
@@ -487,12 +531,12 @@ struct AdjLayout {  // byte offsets of the dynamic shared memory
         BB = 16 * NT * Epad;
         AB = 2 * NCH * 16;
         PS = ms * Jp * 8;
-        oA = 2 * BB;
+        oA = C::NB * BB;
         oP = oA + C::NA * AB;
         oBand = oP + C::NP * PS;
         oF = oBand + 16 * RBW;
         oBar = (oF + 4 * fchunk + 7) & ~7;
-        total = static_cast<size_t>(oBar) + 8 * (2 * C::NA + 2 * C::NP + 13) + 16;
+        total = static_cast<size_t>(oBar) + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 9) + 16;
     }
 };
 
@@ -504,9 +548,10 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // the column tile varies fastest: the tiles of one line and frequency chunk run together and
     // share the table rows and incident fields through L2
-    const int z = blockIdx.y, fc = blockIdx.z;
-    const int b0 = blockIdx.x * a.Bt;
-    if (b0 >= a.B) return;  // uniform
+    const int tile = blockIdx.x, zb = blockIdx.y * a.L, fc = blockIdx.z;
+    const int b0 = tile * a.Bt;
+    const int nL = min(a.L, a.Nz - zb);
+    if (b0 >= a.B || nL <= 0) return;  // uniform
     if (__syncthreads_or(tid == 0 && (*reinterpret_cast<volatile int*>(a.status) & 6) != 0)) return;
     const int f_lo = fc * a.fchunk, f_hi = min(f_lo + a.fchunk, a.F);
 
@@ -514,17 +559,19 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     const uint32_t sBv = sbase, sA = sbase + L.oA, sP = sbase + L.oP, sBand = sbase + L.oBand;
     int* sF = reinterpret_cast<int*>(smem + L.oF);
     const uint32_t bar0 = sbase + L.oBar;
-    const uint32_t BFULL = bar0, BEMPTY = bar0 + 16, AFULL = bar0 + 32, AEMPTY = AFULL + 8 * C::NA,
-                   PF = AFULL + 16 * C::NA, PE = PF + 8 * C::NP, ACCF = PF + 16 * C::NP, ACCE = ACCF + 16,
+    const uint32_t BFULL = bar0, BEMPTY = BFULL + 8 * C::NB, AFULL = BEMPTY + 8 * C::NB, AEMPTY = AFULL + 8 * C::NA,
+                   PF = AEMPTY + 8 * C::NA, PE = PF + 8 * C::NP, ACCF = PE + 8 * C::NP, ACCE = ACCF + 16,
                    BANDF = ACCF + 32, BANDE = ACCF + 48, DRAIN = ACCF + 64;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NA + 2 * C::NP + 13));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 9));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
     volatile int* nfa_s = reinterpret_cast<volatile int*>(tslot + 2);
 
     if (tid == 0) {
-        for (int k = 0; k < 2; ++k) {
-            tc::bar_init(BFULL + 8 * k, kProd);
+        for (int k = 0; k < C::NB; ++k) {
+            tc::bar_init(BFULL + 8 * k, 1);
             tc::bar_init(BEMPTY + 8 * k, 1);
+        }
+        for (int k = 0; k < 2; ++k) {
             tc::bar_init(ACCF + 8 * k, 1);
             tc::bar_init(ACCE + 8 * k, kProd);
             tc::bar_init(BANDF + 8 * k, 1);
@@ -558,7 +605,9 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
     const int nfa = *nfa_s;
-    const int U = 4 * nfa;
+    const int upf = 4 * nL;  // units per frequency: lines x residues
+    const int U = upf * nfa;
+    const int nq = nL * nfa;  // table rows (frequency, line) in order
     const int NCH = L.NCH;
     const int SBOB = 32 * a.Epad;
     int zero = 0;
@@ -569,8 +618,9 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             constexpr uint32_t id_hi = tc::idesc_bf16(128, 4 * NT), id_lo = tc::idesc_bf16(128, 2 * NT);
             const int ksteps = a.Epad / 8;
             for (int u = 0; u < U; ++u) {
-                const int fi = u >> 2, r = u & 3, bb = fi & 1;
-                if (r == 0 && !(ok = tc::bar_wait_abortable(BFULL + 8 * bb, (fi >> 1) & 1, abort_flag, kWaitLimitNs)))
+                const int fi = u / upf, rem = u - fi * upf, zi = rem >> 2, r = rem & 3, kb = fi % C::NB;
+                if (zi == 0 && r == 0 &&
+                    !(ok = tc::bar_wait_abortable(BFULL + 8 * kb, (fi / C::NB) & 1, abort_flag, kWaitLimitNs)))
                     break;
                 const int sa = u % C::NA;
                 if (!(ok = tc::bar_wait_abortable(AFULL + 8 * sa, (u / C::NA) & 1, abort_flag, kWaitLimitNs))) break;
@@ -579,7 +629,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                     break;
                 tc::fence_after_sync();
                 const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
-                const uint32_t ah = sA + sa * L.AB, al = ah + NCH * 16, bv = sBv + bb * L.BB;
+                const uint32_t ah = sA + sa * L.AB, al = ah + NCH * 16, bv = sBv + kb * L.BB;
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const uint64_t dh = tc::smem_desc(ah + 128u * ks, 64, 128);
                     const uint64_t dl = tc::smem_desc(al + 128u * ks, 64, 128);
@@ -589,53 +639,73 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                 }
                 tc::commit(AEMPTY + 8 * sa);
                 tc::commit(ACCF + 8 * acc);
-                if (r == 3) tc::commit(BEMPTY + 8 * bb);
+                if (zi == nL - 1 && r == 3) tc::commit(BEMPTY + 8 * kb);
             }
             tc::commit(DRAIN);
             tc::bar_wait_abortable(DRAIN, 0, &zero, kWaitLimitNs);
             if (!ok) atomicOr(a.status, 4);
         }
     } else if (warp == 9) {
-        if (lane == 0) {  // ---- bulk copies: table rows per frequency, incident fields per unit ----
+        if (lane == 0) {  // ---- bulk copies: V tiles per frequency, table rows per line, incident fields per unit ----
             bool ok = true;
-            int last_p[C::NP], last_band[2] = {-1, -1};
+            int last_p[C::NP], last_b[C::NB], last_band[2] = {-1, -1};
 #pragma unroll
             for (int s = 0; s < C::NP; ++s) last_p[s] = -1;
-            auto band = [&](int fi) {
-                const int bb = fi & 1;
+#pragma unroll
+            for (int s = 0; s < C::NB; ++s) last_b[s] = -1;
+            auto band = [&](int q) {
+                const int bb = q & 1;
                 const uint32_t bytes = 4u * a.RowW;
                 tc::bar_expect_tx(BANDF + 8 * bb, 2 * bytes);
-                const int64_t row = static_cast<int64_t>(sF[fi]) * a.Nz + z;
+                const int64_t row = static_cast<int64_t>(sF[q / nL]) * a.Nz + zb + q % nL;
                 for (int v = 0; v < 2; ++v)
                     tc::bulk_g2s(sBand + (bb * 2 + v) * a.RBW * 4u, a.tr + v * a.tr_vstride + row * a.RowW, bytes,
                                  BANDF + 8 * bb);
-                last_band[bb] = fi >> 1;
+                last_band[bb] = q >> 1;
             };
-            if (nfa > 0) band(0);
-            if (nfa > 1) band(1);
+            auto vtile = [&](int fi) {
+                const int kb = fi % C::NB;
+                tc::bar_expect_tx(BFULL + 8 * kb, L.BB);
+                tc::bulk_g2s(sBv + kb * L.BB, a.vs + (static_cast<int64_t>(sF[fi]) * a.tiles + blockIdx.x) * (L.BB / 4), L.BB,
+                             BFULL + 8 * kb);
+                last_b[kb] = fi / C::NB;
+            };
+            if (nq > 0) band(0);
+            if (nq > 1) band(1);
+            for (int fi = 0; fi < C::NB && fi < nfa; ++fi) vtile(fi);
             const uint32_t seg = 8u * a.Jp;
             for (int u = 0; u < U; ++u) {
-                const int fi = u >> 2, r = u & 3;
+                const int fi = u / upf, rem = u - fi * upf, zi = rem >> 2, r = rem & 3, q = fi * nL + zi;
+                // V tile of frequency fi into the buffer of fi-NB once that frequency's MMAs are done
+                if (zi == 0 && r == 0 && fi >= C::NB) {
+                    if (!(ok = tc::bar_wait_abortable(BEMPTY + 8 * (fi % C::NB), ((fi / C::NB) - 1) & 1, abort_flag,
+                                                      kWaitLimitNs)))
+                        break;
+                    vtile(fi);
+                }
+                // rows of table row q+1 go into the buffer of q-1 once the producers have spread it
+                if (r == 0 && q >= 1 && q + 1 < nq) {
+                    if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((q + 1) & 1), (((q + 1) >> 1) - 1) & 1, abort_flag,
+                                                      kWaitLimitNs)))
+                        break;
+                    band(q + 1);
+                }
                 const int pu = u % C::NP;
                 if (u >= C::NP &&
                     !(ok = tc::bar_wait_abortable(PE + 8 * pu, ((u / C::NP) - 1) & 1, abort_flag, kWaitLimitNs)))
                     break;
-                // rows of frequency fi+1 go into the buffer of fi-1 once the producers have spread it
-                if (r == 0 && fi >= 1 && fi + 1 < nfa) {
-                    if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((fi + 1) & 1), (((fi + 1) >> 1) - 1) & 1, abort_flag,
-                                                      kWaitLimitNs)))
-                        break;
-                    band(fi + 1);
-                }
                 const int f = sF[fi];
                 const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
                 tc::bar_expect_tx(PF + 8 * pu, ns * seg);
-                tc::bulk_g2s(sP + pu * L.PS, a.p_ad + ((static_cast<int64_t>(f) * a.Nz + z) * 4 + r) * a.ms * a.Jp, ns * seg,
-                             PF + 8 * pu);
+                tc::bulk_g2s(sP + pu * L.PS, a.p_ad + ((static_cast<int64_t>(f) * a.Nz + zb + zi) * 4 + r) * a.ms * a.Jp,
+                             ns * seg, PF + 8 * pu);
                 last_p[pu] = u / C::NP;
             }
+            // every copy issued must have landed before the block may exit
             for (int s = 0; s < C::NP; ++s)
                 if (last_p[s] >= 0) tc::bar_wait_abortable(PF + 8 * s, last_p[s] & 1, &zero, kWaitLimitNs);
+            for (int s = 0; s < C::NB; ++s)
+                if (last_b[s] >= 0) tc::bar_wait_abortable(BFULL + 8 * s, last_b[s] & 1, &zero, kWaitLimitNs);
             for (int k = 0; k < 2; ++k)
                 if (last_band[k] >= 0) tc::bar_wait_abortable(BANDF + 8 * k, last_band[k] & 1, &zero, kWaitLimitNs);
             if (!ok) atomicOr(a.status, 4);
@@ -644,46 +714,22 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
         const int qd = warp & 3, h = warp >> 2;
         const int j = qd * 32 + lane;
         const uint32_t lane_addr = static_cast<uint32_t>(qd * 32) << 16;
-        constexpr int NH = NT / 2;
-        // the half's object and its first slot column: Bt == 1 -> both halves serve object b0
-        const int hb = (a.Bt == 2) ? h : 0, hs = (a.Bt == 2) ? 0 : h * NH;
-        const bool hvalid = b0 + hb < a.B;
-        float gx[4], gy[4];  // gamma_hat of x = r + 4j for the half's object
+        constexpr int NH = NT / 2;                      // columns of this half
+        constexpr int MW = NH < 16 ? NH : 16;           // columns per pass
+        constexpr int NPS = NH / MW;                    // passes; pass ps holds one object of the tile
+        const int per = cols_per_object<NT>(a.Bt);
+        float gx[C::MAXL][4][NPS], gy[C::MAXL][4][NPS];  // gamma_hat of x = r + 4j, line zi, pass object
 #pragma unroll
-        for (int rr = 0; rr < 4; ++rr) gx[rr] = gy[rr] = 0.f;
+        for (int zz = 0; zz < C::MAXL; ++zz)
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                for (int ps = 0; ps < NPS; ++ps) gx[zz][rr][ps] = gy[zz][rr][ps] = 0.f;
         bool ok = true;
         for (int it = 0; it < U + C::LAG && ok; ++it) {
             if (it < U) {
-                const int fi = it >> 2, r = it & 3, bb = fi & 1;
-                if (r == 0) {
-                    const int f = sF[fi];
-                    const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
-                    if (fi >= 2 && !(ok = warp_wait(BEMPTY + 8 * bb, ((fi >> 1) - 1) & 1, abort_flag))) break;
-                    // ---- V tile of frequency f -> B buffer bb ----
-                    const uint32_t bv = sBv + bb * L.BB;
-                    const int nblk = (NT / 8) * (a.Epad / 16);
-                    for (int ib = warp; ib < nblk; ib += 8) {
-                        const int cb = ib % (NT / 8), gb = ib / (NT / 8);
-                        const int c = 8 * cb + (lane & 7), g = 4 * gb + (lane >> 3);
-                        int sl, b;
-                        column<NT>(c, ns, s0, b0, a.Bt, a.B, a.f_slot_list, sl, b);
-                        uint32_t hw[4], lw[4];
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            const int e = a.Ex - 1 - (4 * g + t);
-                            float2 v = make_float2(0.f, 0.f);
-                            if (sl >= 0 && e >= 0) v = __ldg(a.V + (static_cast<int64_t>(sl) * a.B + b) * a.E + e);
-                            split(v.x, v.y, hw[t], lw[t]);
-                        }
-                        sts128(bv + b_off(c, g, SBOB), hw[0], hw[1], hw[2], hw[3]);
-                        sts128(bv + b_off(NT + c, g, SBOB), rot(hw[0]), rot(hw[1]), rot(hw[2]), rot(hw[3]));
-                        sts128(bv + b_off(2 * NT + c, g, SBOB), lw[0], lw[1], lw[2], lw[3]);
-                        sts128(bv + b_off(3 * NT + c, g, SBOB), rot(lw[0]), rot(lw[1]), rot(lw[2]), rot(lw[3]));
-                    }
-                    tc::fence_async_smem();
-                    tc::bar_arrive(BFULL + 8 * bb);
-                    if (!(ok = warp_wait(BANDF + 8 * bb, (fi >> 1) & 1, abort_flag))) break;
-                }
+                const int fi = it / upf, rem = it - fi * upf, zi = rem >> 2, r = rem & 3, q = fi * nL + zi, bb = q & 1;
+                if (r == 0 && !(ok = warp_wait(BANDF + 8 * bb, (q >> 1) & 1, abort_flag))) break;
                 // ---- spread chunks of residue r -> A stage ----
                 const int sa = it % C::NA;
                 if (it >= C::NA && !(ok = warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag))) break;
@@ -691,93 +737,113 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                 for (int idx = tid; idx < 2 * NCH; idx += kProd) {
                     const int v = idx >= NCH ? 1 : 0, i = idx - v * NCH;
                     const uint32_t row = sBand + (bb * 2 + v) * a.RBW * 4u + 4u * (r + 4 * i);
-                    sts128(as + 16u * idx, lds32(row), lds32(row + 16), lds32(row + 32), lds32(row + 48));
+                    uint32_t w0, w1, w2, w3;
+                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w0) : "r"(row) : "memory");
+                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w1) : "r"(row + 16) : "memory");
+                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w2) : "r"(row + 32) : "memory");
+                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w3) : "r"(row + 48) : "memory");
+                    sts128(as + 16u * idx, w0, w1, w2, w3);
                 }
-                tc::fence_async_smem();
+                tc::fence_async_smem();  // orders these generic accesses before the MMAs and the next row copy
                 tc::bar_arrive(AFULL + 8 * sa);
                 if (r == 3) tc::bar_arrive(BANDE + 8 * bb);
             }
             // ---- epilogue of unit ue ----
             const int ue = it - C::LAG;
             if (ue >= 0) {
-                const int fi = ue >> 2, r = ue & 3, accs = ue & 1, pu = ue % C::NP;
+                const int fi = ue / upf, rem = ue - fi * upf, zi = rem >> 2, r = rem & 3;
+                const int accs = ue & 1, pu = ue % C::NP;
                 const int f = sF[fi];
-                const int s0 = a.f_slot_ptr[f], ns = a.f_slot_ptr[f + 1] - s0;
+                const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
                 const bool xin = r + 4 * j < a.Nx;
                 if (!(ok = warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag))) break;
-                float2 pv[NH];
+                float2 pv[NPS][MW];
 #pragma unroll
-                for (int m = 0; m < NH; ++m) {
-                    const int sl = hs + m;
-                    pv[m] = make_float2(0.f, 0.f);  // unused columns contribute zero
-                    if (sl < ns && hvalid && xin)
-                        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
-                                     : "=f"(pv[m].x), "=f"(pv[m].y)
-                                     : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
-                }
+                for (int ps = 0; ps < NPS; ++ps)
+#pragma unroll
+                    for (int m = 0; m < MW; ++m) {
+                        const int c = h * NH + ps * MW + m, bl = c / per, sl = c - bl * per;
+                        pv[ps][m] = make_float2(0.f, 0.f);  // unused columns contribute zero
+                        if (sl < ns && b0 + bl < a.B && xin)
+                            asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                                         : "=f"(pv[ps][m].x), "=f"(pv[ps][m].y)
+                                         : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
+                    }
                 tc::fence_async_smem();  // generic reads before the next bulk copy into this stage
                 tc::bar_arrive(PE + 8 * pu);
                 if (!(ok = warp_wait(ACCF + 8 * accs, (ue >> 1) & 1, abort_flag))) break;
                 tc::fence_after_sync();
-                const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NH);
-                float d0[NH], d1[NH], d2[NH], d3[NH];
-                if constexpr (NH == 16) {
-                    tc::tmem_ld16(col, d0);
-                    tc::tmem_ld16(col + NT, d1);
-                    tc::tmem_ld16(col + 2 * NT, d2);
-                    tc::tmem_ld16(col + 3 * NT, d3);
-                } else {
-                    tc::tmem_ld8(col, d0);
-                    tc::tmem_ld8(col + NT, d1);
-                    tc::tmem_ld8(col + 2 * NT, d2);
-                    tc::tmem_ld8(col + 3 * NT, d3);
+#pragma unroll
+                for (int ps = 0; ps < NPS; ++ps) {
+                    const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NH + ps * MW);
+                    float d0[MW], d1[MW], d2[MW], d3[MW];
+                    if constexpr (MW == 16) {
+                        tc::tmem_ld16(col, d0);
+                        tc::tmem_ld16(col + NT, d1);
+                        tc::tmem_ld16(col + 2 * NT, d2);
+                        tc::tmem_ld16(col + 3 * NT, d3);
+                    } else {
+                        tc::tmem_ld8(col, d0);
+                        tc::tmem_ld8(col + NT, d1);
+                        tc::tmem_ld8(col + 2 * NT, d2);
+                        tc::tmem_ld8(col + 3 * NT, d3);
+                    }
+                    tc::tmem_wait_ld();
+                    float sx = 0.f, sy = 0.f;
+#pragma unroll
+                    for (int m = 0; m < MW; ++m) {
+                        const float zr = d0[m] + d2[m], zi2 = -(d1[m] + d3[m]);
+                        const float px = pv[ps][m].x, py = pv[ps][m].y;
+                        sx = fmaf(px, zr, fmaf(py, zi2, sx));  // conj(p) * Z
+                        sy = fmaf(px, zi2, fmaf(-py, zr, sy));
+                    }
+#pragma unroll
+                    for (int zz = 0; zz < C::MAXL; ++zz)
+#pragma unroll
+                        for (int rr = 0; rr < 4; ++rr)
+                            if (zz == zi && rr == r) {
+                                gx[zz][rr][ps] += sx;
+                                gy[zz][rr][ps] += sy;
+                            }
                 }
-                tc::tmem_wait_ld();
                 tc::fence_before_sync();
                 tc::bar_arrive(ACCE + 8 * accs);
-                float sx = 0.f, sy = 0.f;
-#pragma unroll
-                for (int m = 0; m < NH; ++m) {
-                    const float zr = d0[m] + d2[m], zi = -(d1[m] + d3[m]);
-                    const float px = pv[m].x, py = pv[m].y;
-                    sx = fmaf(px, zr, fmaf(py, zi, sx));  // conj(p) * Z
-                    sy = fmaf(px, zi, fmaf(-py, zr, sy));
-                }
-#pragma unroll
-                for (int rr = 0; rr < 4; ++rr)
-                    if (rr == r) {
-                        gx[rr] += sx;
-                        gy[rr] += sy;
-                    }
             }
         }
         if (!ok) atomicOr(a.status, 4);
-        // every MMA has completed (the last epilogue waited on it): the B buffers hold the
-        // two halves' gamma_hat, [h][bb][x]
+        // every MMA has completed (the last epilogue waited on it): the V buffers now hold the
+        // partial gamma_hat of each (half, pass): sG[h*NPS + ps][zi][x]
         producers_sync();
-        float2* sG = reinterpret_cast<float2*>(smem);  // [h][x]
+        float2* sG = reinterpret_cast<float2*>(smem);
         const bool good = !*abort_flag;
         if (good) {
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) {
-                const int x = rr + 4 * j;
-                if (x < a.Nx) sG[static_cast<size_t>(h) * a.Nx + x] = make_float2(gx[rr], gy[rr]);
-            }
+            for (int zz = 0; zz < C::MAXL; ++zz)
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                    for (int ps = 0; ps < NPS; ++ps) {
+                        const int x = rr + 4 * j;
+                        if (zz < nL && x < a.Nx)
+                            sG[((static_cast<size_t>(h) * NPS + ps) * a.L + zz) * a.Nx + x] =
+                                make_float2(gx[zz][rr][ps], gy[zz][rr][ps]);
+                    }
         }
         producers_sync();
         if (good) {
-            const int64_t line_pt = static_cast<int64_t>(z) * a.Nx;
-            if (a.Bt == 1) {  // both halves hold parts of object b0
-                for (int x = tid; x < a.Nx; x += kProd) {
-                    const float2 g0 = sG[x], g1 = sG[a.Nx + x];
-                    a.part[(static_cast<int64_t>(fc) * a.B + b0) * a.P + line_pt + x] = make_float2(g0.x + g1.x, g0.y + g1.y);
+            const int nb = min(a.Bt, a.B - b0);
+            for (int idx = tid; idx < nb * nL * a.Nx; idx += kProd) {
+                const int bl = idx / (nL * a.Nx), rest = idx - bl * (nL * a.Nx), zz = rest / a.Nx, x = rest - zz * a.Nx;
+                float2 s = make_float2(0.f, 0.f);
+                for (int k = 0; k < 2 * NPS; ++k) {  // (half, pass) slots whose columns belong to object bl
+                    const int c0 = (k / NPS) * NH + (k % NPS) * MW;
+                    if (c0 / per == bl) {
+                        const float2 v = sG[(static_cast<size_t>(k) * a.L + zz) * a.Nx + x];
+                        s.x += v.x;
+                        s.y += v.y;
+                    }
                 }
-            } else {
-                const int nb = min(2, a.B - b0);
-                for (int idx = tid; idx < nb * a.Nx; idx += kProd) {
-                    const int bl = idx / a.Nx, x = idx - bl * a.Nx;
-                    a.part[(static_cast<int64_t>(fc) * a.B + b0 + bl) * a.P + line_pt + x] = sG[static_cast<size_t>(bl) * a.Nx + x];
-                }
+                a.part[(static_cast<int64_t>(fc) * a.B + b0 + bl) * a.P + static_cast<int64_t>(zb + zz) * a.Nx + x] = s;
             }
         }
     }
@@ -858,11 +924,12 @@ Tile2 tile2(const Plan* p, int B) {
     return t;
 }
 
-// forward tiles: 64 columns (4 objects x up to 16 waves, N = 256 per MMA) when the batch fills them,
-// so that each staged table row feeds twice the columns; otherwise the adjoint's tiles
+// column tiles of both kernels: 64 columns (4 objects x up to 16 waves, N = 256 per MMA) when the
+// batch fills them, so that each staged table row feeds twice the columns; otherwise tile2
 Tile2 tile_fwd(const Plan* p, int B) {
     const int ms = std::max(1, p->max_slots_per_f);
-    if (B >= 4 && ms >= 12 && ms <= 16) {
+    // (the adjoint's final gamma_hat of 2 lines x 4 column slots reuses its 16*64*Epad-byte V buffer)
+    if (B >= 4 && ms >= 12 && ms <= 16 && p->Nx <= 16 * ((p->Ex + 15) / 16 * 16)) {
         Tile2 t;
         t.NT = 64, t.Bt = 4, t.tiles = (B + 3) / 4;
         return t;
@@ -909,22 +976,32 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
 
 template <int NT>
 cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nfc_out) {
+    const int Lz = (NT >= 64) ? AdjCfg<NT>::MAXL : 1;  // grid lines per block
+    const int zblocks = (p->Nz + Lz - 1) / Lz;
     const size_t slab = static_cast<size_t>(B) * p->P * sizeof(float2);
-    int nfc = std::max(1, std::min(p->F, (8 * 152 + p->Nz * t.tiles - 1) / (p->Nz * t.tiles)));
+    int nfc = std::max(1, std::min(p->F, (8 * 152 + zblocks * t.tiles - 1) / (zblocks * t.tiles)));
     nfc = static_cast<int>(std::max<size_t>(1, std::min<size_t>(nfc, p->ws_part_bytes / std::max<size_t>(slab, 1))));
     const int fchunk = (p->F + nfc - 1) / nfc;
     nfc = (p->F + fchunk - 1) / fchunk;
+    // V (unmixed data) -> split bf16 tiles in the B-operand layout, one per (frequency, column tile)
+    const int64_t nv = static_cast<int64_t>(p->F) * t.tiles * NT * (p->Epad / 4);
+    vsplit_kernel<NT><<<static_cast<int>(std::min<int64_t>((nv + 255) / 256, 152 * 32)), 256, 0, st>>>(
+        p->ws_G, p->f_slot_ptr, p->f_slot_list, p->ws_vs, p->F, t.tiles, t.Bt, B, p->E, p->Ex, p->Epad);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     Adj2Args a;
     a.tr = p->tr; a.tr_vstride = p->tr_vstride; a.RowW = p->RowW; a.RBW = tc2_rbw(p);
-    a.p_ad = p->p_ad; a.Jp = p->Jp; a.V = p->ws_G; a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
+    a.p_ad = p->p_ad; a.Jp = p->Jp; a.vs = p->ws_vs; a.tiles = t.tiles;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.Epad = p->Epad; a.B = B; a.Bt = t.Bt; a.F = p->F;
-    a.fchunk = fchunk; a.ms = p->ms; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
+    a.fchunk = fchunk; a.ms = p->ms; a.L = Lz; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
-    cudaError_t e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(L.total));
-    if (e != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(L.total))) != cudaSuccess)
+        return e;
     if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
-    adj_tc2_kernel<NT><<<dim3(t.tiles, p->Nz, nfc), kThreads2, L.total, st>>>(a);
+    adj_tc2_kernel<NT><<<dim3(t.tiles, zblocks, nfc), kThreads2, L.total, st>>>(a);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *nfc_out = nfc;
@@ -942,7 +1019,8 @@ size_t tc2_smem_need(const Plan* p, int Epad, int RowW) {
     size_t need = 0;
     for (int B = 1; B <= std::min(p->max_objects, 4); ++B) {
         const Tile2 tf = tile_fwd(p, B);
-        if (tf.NT == 64) need = std::max(need, FwdLayout<64>(ms, tf.Bt, rbw).total);
+        if (tf.NT == 64)
+            need = std::max({need, FwdLayout<64>(ms, tf.Bt, rbw).total, AdjLayout<64>(Epad, rbw, ms, Jp, p->F).total});
         const Tile2 t = tile2(p, B);
         if (t.NT == 16)
             need = std::max({need, FwdLayout<16>(ms, t.Bt, rbw).total, AdjLayout<16>(Epad, rbw, ms, Jp, p->F).total});
@@ -992,6 +1070,12 @@ cui_status tc2_prepare(Plan& p) {
     if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_ad), sizeof(float2) * ad_elems)) != CUI_OK) return st;
     if ((st = device_alloc(p, reinterpret_cast<void**>(&p.ws_galign), sizeof(float2) * p.P * p.max_objects)) != CUI_OK)
         return st;
+    size_t vs_bytes = 0;  // split V tiles of the largest apply: F x tiles x 16 NT Epad bytes
+    for (int B = 1; B <= p.max_objects; ++B) {
+        const Tile2 t = tile_fwd(&p, B);
+        vs_bytes = std::max(vs_bytes, static_cast<size_t>(p.F) * t.tiles * 16 * t.NT * p.Epad);
+    }
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.ws_vs), vs_bytes)) != CUI_OK) return st;
     int blocks = static_cast<int>(std::min<int64_t>((p.tr_vstride + 255) / 256, 152 * 32));
     row_kernel<<<blocks, 256>>>(p.table, p.tr, n_rows, p.Nox, p.RowW, p.tr_vstride);
     count_launch();
@@ -1004,7 +1088,7 @@ cui_status tc2_prepare(Plan& p) {
     if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "slot-major incident fields");
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return check_cuda(e, "line-unit tables");
     p.tc_bytes += sizeof(uint32_t) * 2 * static_cast<size_t>(p.tr_vstride) + sizeof(float2) * (fw_elems + ad_elems) +
-                  sizeof(float2) * p.P * p.max_objects;
+                  sizeof(float2) * p.P * p.max_objects + vs_bytes;
     p.tc2 = 1;
     return CUI_OK;
 }
@@ -1016,7 +1100,8 @@ cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cud
 }
 
 cudaError_t launch_adj_tc2(Plan* p, int B, cudaStream_t st, int* nfc) {
-    const Tile2 t = tile2(p, B);
+    const Tile2 t = tile_fwd(p, B);  // the adjoint uses the forward's column tiles
+    if (t.NT == 64) return launch_adj2<64>(p, B, t, st, nfc);
     return t.NT == 16 ? launch_adj2<16>(p, B, t, st, nfc) : launch_adj2<32>(p, B, t, st, nfc);
 }
 
