@@ -355,3 +355,30 @@ def test_autotune_keeps_a_path_that_matches_oracle(name):
     u = op.forward(dev(gamma)).cpu().numpy()
     assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
     assert op.device_status() == 0
+
+
+@pytest.mark.parametrize("n_lines,n_obj", [(17, 6), (9, 5)])
+def test_bf16x3_wide_tiles_partial_tile_and_odd_lines(n_lines, n_obj):
+    """64-column tiles (4 objects x 16 waves): the last tile only partly filled (objects not a
+    multiple of 4) and an odd number of grid lines (the adjoint's last block covers one line
+    of its two).  Compared per object with the FP32 path of the same plan; bound 1e-5."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload("2d-batched")
+    w.f = w.f[:2]
+    w.n_points_axis = (w.n_points_axis[0], n_lines)
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
+    rng = np.random.default_rng(5)
+    g = rng.standard_normal((op.n_points, n_obj)) + 1j * rng.standard_normal((op.n_points, n_obj))
+    y = rng.standard_normal((op.n_observations, n_obj)) + 1j * rng.standard_normal((op.n_observations, n_obj))
+    u32 = op.forward(dev(g)).cpu().numpy()
+    a32 = op.adjoint(dev(y)).cpu().numpy()
+    op.set_precision("bf16x3")
+    u16 = op.forward(dev(g)).cpu().numpy()
+    a16 = op.adjoint(dev(y)).cpu().numpy()
+    assert op.device_status() == 0
+    for b in range(n_obj):
+        assert rel_l2(u16[:, b], u32[:, b]) <= TOL
+        assert rel_l2(a16[:, b], a32[:, b]) <= TOL
+    op.close()
