@@ -367,6 +367,15 @@ def run_ours(args):
         line["fp32_comparison"] = {"value": v32, "unit": "applies/s", "ms_per_step": ms32, "steps": args.fp32_steps,
                                    "speedup_bf16x3_over_fp32": value / v32,
                                    "rel_l2_grad_bf16x3_vs_fp32": (accuracy or {}).get("rel_l2_grad_vs_fp32")}
+    # received energies ||Phi e_p||^2 of the same plan (energy_rx, once per operator in the reference's solvers)
+    op.energy_rx()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.current_stream())
+    op.energy_rx()
+    e1.record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    line["energy_rx_ms"] = e0.elapsed_time(e1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload, B)

@@ -121,6 +121,7 @@ _SIGNATURES = {
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
     "cui_born_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "cui_born_energy_rx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "cui_born_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
     "cui_born_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -517,6 +518,14 @@ class OperatorBorn:
         self.lasso_(gc, uc, lam_t, step, n_iter, loss)
         g = gc.t()
         return (g[:, 0], loss[0]) if vec else (g, loss)
+
+    def energy_rx(self):
+        """Received energies ``||Phi e_p||^2`` of every grid point (``cui_born_energy_rx``,
+        ``operator_born.m:718-859``): a float32 CUDA tensor of N_points values."""
+        import torch
+        out = torch.empty(self.n_points, dtype=torch.float32, device="cuda")
+        _check(self._lib.cui_born_energy_rx(self._plan, out.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        return out
 
     def norm_estimate(self, n_iter: int = 20, seed: int = 0) -> float:
         """||Phi||_2^2 by power iteration on Phi^H Phi (device applies)."""

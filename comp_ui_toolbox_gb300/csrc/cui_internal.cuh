@@ -64,6 +64,7 @@ struct Plan {
     float2* p_in = nullptr;
     int* f_slot_ptr = nullptr;      // [F+1] CSR of slots per global frequency
     int* f_slot_list = nullptr;     // [S]
+    int* slot_f = nullptr;          // [S] global frequency of each slot
     int* row_slot = nullptr;        // [n_obs]
     int* row_mix = nullptr;         // [n_obs]
     int* row_fl = nullptr;          // [n_obs]

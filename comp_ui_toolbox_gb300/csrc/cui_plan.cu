@@ -343,6 +343,7 @@ cui_status select_device_and_shapes(Plan& p, int device) {
 cui_status upload_metadata_and_workspace(Plan& p) {
     HostMeta& h = p.h_meta;
     CUI_TRY(upload(p, &p.f_slot_ptr, p.h_f_slot_ptr));
+    CUI_TRY(upload(p, &p.slot_f, p.h_slot_f));
     CUI_TRY(upload(p, &p.f_slot_list, p.h_f_slot_list));
     CUI_TRY(upload(p, &p.row_slot, h.row_slot));
     CUI_TRY(upload(p, &p.row_mix, h.row_mix));

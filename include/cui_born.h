@@ -226,6 +226,14 @@ cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int6
                           cui_complex32* gamma, int64_t ld_gamma, const float* lambda, float step, int32_t n_iter,
                           float* loss, void* stream);
 
+/* Received energies in the canonical basis, energy_rx of the reference
+ * (+scattering/operator_born.m:718-859, energy_rx_canonical; used to normalise
+ * the operator before a solve, +regularization/+options/common.m:166-184):
+ *   energy[p] = sum over observations of |Phi[row, p]|^2 = ||Phi e_p||^2,
+ * p = 0..N_points-1, written to the device array `energy` (N_points floats).
+ * TGC is the identity.  Allocates nothing; launches only on `stream`. */
+cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, void* stream);
+
 /* ---- host applies (FP64, MEX semantics) ----------------------------------
  * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
  * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).

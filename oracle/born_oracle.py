@@ -530,3 +530,26 @@ def adjoint_quick_cpu(op: OperatorTables, u: np.ndarray) -> np.ndarray:
                 Phi = h_rx * p_act * mix.pref[:, a][:, None]
                 gamma_hat += Phi.conj().T @ u_mix
     return gamma_hat
+
+
+def energy_rx_cpu(op: OperatorTables) -> np.ndarray:
+    """Received energies in the canonical basis, restating ``energy_rx_canonical``
+    (``operator_born.m:718-859``): per measurement and mix, the mixed voltage
+    signals of every grid point ``Phi_M = sum_a h_rx * p_in * pref`` (``:773-836``)
+    and ``E_M += vecnorm(Phi_M, 2, 1).^2`` (``:853``), i.e. ``E[p] = ||Phi e_p||^2``.
+    The reference restricts the method to one selected measurement (``:736-741``);
+    the sum here runs over every selected measurement, which is the same column
+    norm of the stacked operator.  TGC is the identity (out of scope).
+    """
+    P = op.setup.n_points
+    allp = np.arange(P)
+    E = np.zeros(P)
+    for meas in op.measurements:
+        for mix in meas.mixes:
+            f_glob = meas.f_idx[mix.f_idx]
+            p_act = meas.p_incident[mix.f_idx]
+            Phi_M = np.zeros((len(mix.f_idx), P), dtype=np.complex128)
+            for a, e in enumerate(mix.active):
+                Phi_M += op._h_rx(int(e), f_glob, allp) * p_act * mix.pref[:, a][:, None]
+            E += np.sum(np.abs(Phi_M) ** 2, axis=0)
+    return E

@@ -382,3 +382,15 @@ def test_bf16x3_wide_tiles_partial_tile_and_odd_lines(n_lines, n_obj):
         assert rel_l2(u16[:, b], u32[:, b]) <= TOL
         assert rel_l2(a16[:, b], a32[:, b]) <= TOL
     op.close()
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_energy_rx_matches_oracle(name):
+    """Received energies ||Phi e_p||^2 (energy_rx_canonical, operator_born.m:718-859) against the
+    FP64 restatement; bound 1e-5 relative L2."""
+    from oracle.born_oracle import energy_rx_cpu
+    b = built(name)
+    op = make_operator(b, "lateral", max_objects=max(1, b.cfg.n_objects))
+    E = op.energy_rx().cpu().numpy()
+    assert rel_l2(E, energy_rx_cpu(b.op)) <= TOL
+    assert op.device_status() == 0

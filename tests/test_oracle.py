@@ -172,3 +172,16 @@ def test_benchmark_workloads_match_oracle_configs(wname, cname):
     np.testing.assert_array_equal(w.mix_weights(), configs.mix_weights(c))
     assert w.n_objects == c.n_objects and w.density == c.density and w.seed == c.seed
     np.testing.assert_array_equal(w.gamma(n_objects=1), configs.make_gamma(c, n_objects=1))
+
+
+def test_energy_rx_restatement_equals_column_norms():
+    """The energy_rx restatement equals ||Phi e_p||^2 taken from explicit columns of the forward."""
+    from oracle.born_oracle import energy_rx_cpu
+    b = configs.build(configs.small_config("c2"))
+    E = energy_rx_cpu(b.op)
+    P = b.cfg.setup.n_points
+    for p in np.random.default_rng(0).choice(P, 4, replace=False):
+        e = np.zeros((P, 1))
+        e[p] = 1.0
+        col = forward_quick_cpu(b.op, e)
+        assert abs(E[p] - np.sum(np.abs(col) ** 2)) <= 1e-12 * E[p]
