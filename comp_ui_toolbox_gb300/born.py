@@ -122,6 +122,8 @@ _SIGNATURES = {
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
     "cui_born_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "cui_born_energy_rx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cui_born_omp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int64), C.c_void_p,
+                               C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_void_p]),
     "cui_born_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
     "cui_born_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -526,6 +528,21 @@ class OperatorBorn:
         out = torch.empty(self.n_points, dtype=torch.float32, device="cuda")
         _check(self._lib.cui_born_energy_rx(self._plan, out.data_ptr(), torch.cuda.current_stream().cuda_stream))
         return out
+
+    def omp(self, y, n_atoms_max: int, rel_rmse: float = 0.0):
+        """Orthogonal matching pursuit (``cui_born_omp``, ``omp.m:161-200``) on one measured
+        column ``y`` (CUDA complex64, N_obs values): returns ``(atoms, coefficients,
+        rel_residuals)`` as numpy arrays of the number of atoms taken."""
+        import torch
+        yc = y.reshape(-1).contiguous()
+        atoms = (C.c_int64 * n_atoms_max)()
+        coeff = np.zeros(n_atoms_max, dtype=np.complex64)
+        res = (C.c_float * n_atoms_max)()
+        n = C.c_int32(0)
+        _check(self._lib.cui_born_omp(self._plan, yc.data_ptr(), int(n_atoms_max), float(rel_rmse), atoms,
+                                      coeff.ctypes.data, res, C.byref(n), torch.cuda.current_stream().cuda_stream))
+        k = n.value
+        return np.array(atoms[:k], dtype=np.int64), coeff[:k].copy(), np.array(res[:k], dtype=np.float32)
 
     def norm_estimate(self, n_iter: int = 20, seed: int = 0) -> float:
         """||Phi||_2^2 by power iteration on Phi^H Phi (device applies)."""

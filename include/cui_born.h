@@ -234,6 +234,25 @@ cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int6
  * TGC is the identity.  Allocates nothing; launches only on `stream`. */
 cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, void* stream);
 
+/* Orthogonal matching pursuit on one measured column, omp.m of the reference
+ * (+regularization/+algorithms/+greedy/omp.m:161-200, reached through
+ * +scattering/operator.m:601-790 with op_A = combined_scalar):
+ *   per iteration the atom maximising |Phi^H r| (ties to the smaller index),
+ *   the least-squares coefficients of y on the atoms so far, and the residual
+ *   r = y - Phi_sel c; stops after n_atoms_max atoms or once ||r|| / ||y||
+ *   <= rel_rmse (omp.m:215).
+ * `y` is a device array of N_obs values.  Host outputs: `atoms` (n_atoms_max
+ * grid-point indices, 0-based), `coefficients` (n_atoms_max), `rel_residuals`
+ * (n_atoms_max, may be NULL: ||r|| / ||y|| after each atom), `*n_atoms` the
+ * number of atoms taken.  The least squares is kept as an orthonormal basis of
+ * the selected columns (Gram-Schmidt, twice); the columns come straight from
+ * the tables, not from a forward apply.  Allocates device scratch of about
+ * (n_atoms_max + 3) * N_obs + N_points complex values per call and
+ * synchronises `stream` once per iteration. */
+cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, int32_t n_atoms_max, float rel_rmse,
+                        int64_t* atoms, cui_complex32* coefficients, float* rel_residuals, int32_t* n_atoms,
+                        void* stream);
+
 /* ---- host applies (FP64, MEX semantics) ----------------------------------
  * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
  * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).

@@ -1,7 +1,8 @@
 """FP64 restatement of the solver loop that drives the Born operator (test infrastructure).
 
 TEST INFRASTRUCTURE ONLY: used by ``tests/`` as the checker of the library's
-device LASSO iterations (``cui_born_lasso``); nothing in the product imports it.
+device LASSO iterations (``cui_born_lasso``) and orthogonal matching pursuit
+(``cui_born_omp``); nothing in the product imports it.
 
 The reference solves its sparse-recovery problems through
 ``operator.lq_minimization`` (``+scattering/operator.m:601-790``), which wraps
@@ -16,6 +17,7 @@ workload runs the plainest member of that family, proximal-gradient LASSO
     gamma <- S(gamma - t Phi^H (Phi gamma - u), t lambda),  S(v, s) = v max(0, 1 - s/|v|)
 
 which is what :func:`lasso_ista` restates with the oracle's FP64 operator.
+:func:`omp_cpu` restates the greedy member, ``omp.m``.
 """
 
 from __future__ import annotations
@@ -61,3 +63,42 @@ def operator_norm2(op: OperatorTables, n_iter: int = 30, seed: int = 0) -> float
         lam = float(np.linalg.norm(y))
         x = y / lam
     return lam
+
+
+def omp_cpu(op: OperatorTables, y: np.ndarray, n_atoms_max: int, rel_rmse: float = 0.0,
+            path=None):
+    """Orthogonal matching pursuit, restating ``omp.m:161-200`` with the FP64 operator:
+    adjoint of the residual (``:166-171``), atom of largest magnitude (``:174``), the
+    atom's column via a forward of a unit vector (``:177-185``), the normal equations on
+    the atoms so far (``:190-191``) and the residual (``:196-198``); stops once the
+    relative RMSE is reached (``:215``).  Returns ``(atoms, coefficients, rel_residuals)``.
+
+    With ``path`` (a sequence of atoms) the iterations take those atoms instead of the
+    argmax and the function returns ``(atoms, coefficients, rel_residuals, scores)``,
+    ``scores[i]`` being the magnitude of the taken atom in the adjoint of the residual
+    divided by the largest magnitude there (1 for an exact argmax).  It evaluates an
+    atom sequence chosen by a lower-precision implementation."""
+    y = np.asarray(y, dtype=np.complex128).reshape(-1)
+    P = op.setup.n_points
+    y_norm = np.linalg.norm(y)
+    res = y.copy()
+    atoms, cols, rel, scores = [], [], [], []
+    coeff = np.zeros(0, dtype=np.complex128)
+    n_iter = min(n_atoms_max, len(y)) if path is None else len(path)
+    for i in range(n_iter):
+        g = np.abs(adjoint_quick_cpu(op, res[:, None])[:, 0])
+        k = int(np.argmax(g)) if path is None else int(path[i])
+        scores.append(g[k] / g.max())
+        atoms.append(k)
+        e = np.zeros((P, 1))
+        e[k] = 1.0
+        cols.append(forward_quick_cpu(op, e)[:, 0])
+        A = np.stack(cols, axis=1)
+        coeff = np.linalg.solve(A.conj().T @ A, A.conj().T @ y)
+        res = y - A @ coeff
+        rel.append(np.linalg.norm(res) / y_norm)
+        if path is None and rel[-1] <= rel_rmse:
+            break
+    if path is None:
+        return np.array(atoms), coeff, np.array(rel)
+    return np.array(atoms), coeff, np.array(rel), np.array(scores)
