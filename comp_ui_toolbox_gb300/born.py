@@ -124,6 +124,8 @@ _SIGNATURES = {
     "cui_born_energy_rx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "cui_born_omp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int64), C.c_void_p,
                                C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_void_p]),
+    "cui_born_cosamp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int64),
+                                  C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_void_p]),
     "cui_born_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
     "cui_born_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_timing_enable": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -543,6 +545,22 @@ class OperatorBorn:
                                       coeff.ctypes.data, res, C.byref(n), torch.cuda.current_stream().cuda_stream))
         k = n.value
         return np.array(atoms[:k], dtype=np.int64), coeff[:k].copy(), np.array(res[:k], dtype=np.float32)
+
+    def cosamp(self, y, sparsity: int, n_iter_max: int, rel_rmse: float = 0.0):
+        """Compressive sampling matching pursuit (``cui_born_cosamp``, ``cosamp.m:174-272``) on
+        one measured column ``y`` (CUDA complex64, N_obs values): returns ``(atoms,
+        coefficients, rel_residuals)``; atoms and coefficients hold the final ``sparsity``
+        atoms, largest coefficient first, and ``rel_residuals`` one value per iteration run."""
+        import torch
+        yc = y.reshape(-1).contiguous()
+        atoms = (C.c_int64 * sparsity)()
+        coeff = np.zeros(sparsity, dtype=np.complex64)
+        res = (C.c_float * max(1, n_iter_max))()
+        n = C.c_int32(0)
+        _check(self._lib.cui_born_cosamp(self._plan, yc.data_ptr(), int(sparsity), int(n_iter_max), float(rel_rmse),
+                                         atoms, coeff.ctypes.data, res, C.byref(n),
+                                         torch.cuda.current_stream().cuda_stream))
+        return np.array(atoms[:], dtype=np.int64), coeff, np.array(res[:n.value], dtype=np.float32)
 
     def norm_estimate(self, n_iter: int = 20, seed: int = 0) -> float:
         """||Phi||_2^2 by power iteration on Phi^H Phi (device applies)."""

@@ -253,6 +253,26 @@ cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, int32_t n_a
                         int64_t* atoms, cui_complex32* coefficients, float* rel_residuals, int32_t* n_atoms,
                         void* stream);
 
+/* Compressive sampling matching pursuit on one measured column, cosamp.m of the
+ * reference (+regularization/+algorithms/+greedy/cosamp.m:174-272):
+ *   per iteration the 2s largest entries of |Phi^H r| (ties to the smaller
+ *   index), their union with the current s atoms, the least-squares fit of y on
+ *   the union, pruning to the s largest coefficient magnitudes, and the
+ *   residual r = y - Phi_s c_s with the pruned coefficients (not refitted);
+ *   stops after n_iter_max iterations or once ||r|| / ||y|| <= rel_rmse (:270).
+ * s = `sparsity`, 1 <= s <= 512, 2s <= N_points, 3s <= N_obs (else
+ * CUI_ERR_INVALID_ARG).  `y` is a device array of N_obs values.  Host outputs:
+ * `atoms` and `coefficients` (s each: the final support in the reference's
+ * order, largest coefficient first), `rel_residuals` (n_iter_max, may be NULL),
+ * `*n_iter` the iterations run.  The least squares is a device Gram matrix
+ * (FP64 sums) solved by Cholesky in FP64 with two refinement steps;
+ * CUI_ERR_NUMERIC when that Gram matrix is not positive definite.  Allocates
+ * device scratch of about (3s + 2) * N_obs + 2 * N_points values per call and
+ * synchronises `stream` a few times per iteration. */
+cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* y, int32_t sparsity, int32_t n_iter_max,
+                           float rel_rmse, int64_t* atoms, cui_complex32* coefficients, float* rel_residuals,
+                           int32_t* n_iter, void* stream);
+
 /* ---- host applies (FP64, MEX semantics) ----------------------------------
  * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
  * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).

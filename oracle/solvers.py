@@ -102,3 +102,56 @@ def omp_cpu(op: OperatorTables, y: np.ndarray, n_atoms_max: int, rel_rmse: float
     if path is None:
         return np.array(atoms), coeff, np.array(rel)
     return np.array(atoms), coeff, np.array(rel), np.array(scores)
+
+
+def cosamp_cpu(op: OperatorTables, y: np.ndarray, sparsity: int, n_iter_max: int, rel_rmse: float = 0.0,
+               return_margins: bool = False):
+    """Compressive sampling matching pursuit, restating ``cosamp.m:174-272`` with the FP64
+    operator: signal proxy ``Phi^H r`` (``:180-185``), the ``2 s`` largest magnitudes in a
+    stable descending sort (``:188-189``), union with the current atoms in ascending order
+    (``:192-195``), the new atoms' columns via forwards of unit vectors (``:209-228``), the
+    least-squares fit ``A \\ y`` on the union (``:244``), pruning to the ``s`` largest
+    coefficients in a stable descending sort (``:247-249``), the residual with the pruned
+    coefficients, not refitted (``:259-261``), and the relative-RMSE stop (``:270``).
+
+    Returns ``(atoms, coefficients, rel_residuals)``: the final ``s`` atoms in the
+    reference's order (descending coefficient magnitude) and their coefficients.  With
+    ``return_margins`` a fourth item lists, per iteration, the relative gaps at the two
+    selection boundaries (2s-th vs next proxy magnitude, s-th vs next coefficient
+    magnitude) that decide the sets."""
+    y = np.asarray(y, dtype=np.complex128).reshape(-1)
+    P = op.setup.n_points
+    y_norm = np.linalg.norm(y)
+    res = y.copy()
+    atoms = np.zeros(0, dtype=np.int64)
+    cols = {}
+    rel, margins = [], []
+    coeff_kept = np.zeros(0, dtype=np.complex128)
+    n_sel = min(2 * sparsity, P)
+    for _ in range(min(n_iter_max, len(y))):
+        g = np.abs(adjoint_quick_cpu(op, res[:, None])[:, 0])
+        order = np.argsort(-g, kind="stable")
+        ident = order[:n_sel]
+        m_sel = (g[order[n_sel - 1]] / g[order[n_sel]] - 1.0) if n_sel < P else np.inf
+        union = np.union1d(atoms, ident).astype(np.int64)
+        for k in union:
+            if int(k) not in cols:
+                e = np.zeros((P, 1))
+                e[k] = 1.0
+                cols[int(k)] = forward_quick_cpu(op, e)[:, 0]
+        A = np.stack([cols[int(k)] for k in union], axis=1)
+        coeff = np.linalg.lstsq(A, y, rcond=None)[0]
+        mag = np.abs(coeff)
+        keep = np.argsort(-mag, kind="stable")
+        m_prune = (mag[keep[sparsity - 1]] / mag[keep[sparsity]] - 1.0) if sparsity < len(union) else np.inf
+        keep = keep[:sparsity]
+        atoms = union[keep]
+        coeff_kept = coeff[keep]
+        cols = {int(k): cols[int(k)] for k in atoms}
+        res = y - np.stack([cols[int(k)] for k in atoms], axis=1) @ coeff_kept
+        rel.append(np.linalg.norm(res) / y_norm)
+        margins.append((m_sel, m_prune))
+        if rel[-1] <= rel_rmse:
+            break
+    out = (atoms, coeff_kept, np.array(rel))
+    return out + (margins,) if return_margins else out
