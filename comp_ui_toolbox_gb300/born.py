@@ -105,6 +105,9 @@ _lib = None
 _SIGNATURES = {
     "cui_born_plan_create": (C.c_int, [C.POINTER(BornDesc), C.c_int32, C.POINTER(C.c_void_p)]),
     "cui_born_plan_create_setup": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.POINTER(C.c_void_p)]),
+    "cui_born_plan_create_setup_cached": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.c_char_p,
+                                                    C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]),
+    "cui_born_setup_hash": (C.c_int, [C.POINTER(SetupDesc), C.c_char_p]),
     "cui_born_plan_destroy": (C.c_int, [C.c_void_p]),
     "cui_born_plan_info": (C.c_int, [C.c_void_p, C.POINTER(BornInfo)]),
     "cui_born_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -264,66 +267,31 @@ class OperatorBorn:
         self._finish(max_objects, device)
 
     @classmethod
-    def from_setup(cls, *, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_start: float,
-                   n_elements_axis: Sequence[int], pitch_axis: Sequence[float], width_axis: Sequence[float],
-                   n_face_axis: Sequence[int], absorption: dict, f_unique, waves,
-                   aa_tx_beta: Optional[float] = 0.5, aa_rx_beta: Optional[float] = 0.5,
-                   device: int = 0, max_objects: int = 1) -> "OperatorBorn":
-        """Plan whose tables the GPU computes from the discretised setup.
+    def from_setup(cls, *, device: int = 0, max_objects: int = 1, cache_dir: Optional[str] = None,
+                   **setup) -> "OperatorBorn":
+        """Plan whose tables the GPU computes from the discretised setup (``setup_desc`` lists
+        the keyword arguments).
 
-        ``absorption``: ``{"kind": "none"|"time_causal", "c", "constant_db", "slope_db", "exponent",
-        "f_ref", "dispersion"}``.  ``waves``: objects or dicts with ``f_idx`` (0-based global
-        frequency indices), ``v_d`` ``(F_w, E)`` normal velocities and ``mixes`` (``f_idx``,
-        ``active``, ``response`` ``(F_mix, n_active)`` receive responses).  ``aa_*_beta=None``
-        switches an anti-aliasing filter off.
+        With ``cache_dir`` the plan goes through the table cache
+        (``cui_born_plan_create_setup_cached``, ``compute_or_load_hash.m``): the table and the
+        incident fields are loaded from ``cache_dir/cui_born_<setup hash>.tables`` when that
+        file exists, else computed and stored there.  ``loaded_from_cache`` is then 1 (loaded),
+        0 (computed and stored) or -1 (computed; storing failed).
         """
         self = cls.__new__(cls)
         lib = load_library()
         self._lib = lib
         self._plan = C.c_void_p()
-        keep = []
-        d = SetupDesc()
-        nd = len(n_points_axis)
-        d.n_dims = nd
-        for k in range(nd):
-            d.n_points_axis[k] = int(n_points_axis[k])
-            d.delta_axis[k] = float(delta_axis[k])
-        for k in range(nd - 1):
-            d.n_elements_axis[k] = int(n_elements_axis[k])
-            d.pitch_axis[k] = float(pitch_axis[k])
-            d.width_axis[k] = float(width_axis[k])
-            d.n_face_axis[k] = int(n_face_axis[k])
-        d.z_start = float(z_start)
-        a = AbsorptionDesc()
-        a.kind = {"none": 0, "time_causal": 1}[absorption.get("kind", "none")]
-        a.c = float(absorption.get("c", 1500.0))
-        a.constant_db = float(absorption.get("constant_db", 0.0))
-        a.slope_db = float(absorption.get("slope_db", 0.0))
-        a.exponent = float(absorption.get("exponent", 1.0))
-        a.f_ref = float(absorption.get("f_ref", 4e6))
-        a.dispersion = int(bool(absorption.get("dispersion", True)))
-        d.absorption = a
-        d.aa_tx_beta = -1.0 if aa_tx_beta is None else float(aa_tx_beta)
-        d.aa_rx_beta = -1.0 if aa_rx_beta is None else float(aa_rx_beta)
-        f = np.ascontiguousarray(np.asarray(f_unique, dtype=np.float64))
-        keep.append(f)
-        d.n_f_unique = len(f)
-        d.f_unique = f.ctypes.data_as(C.POINTER(C.c_double))
-        wv = (WaveDesc * len(waves))()
-        for w, wave in enumerate(waves):
-            f_idx = _i32(np.asarray(_get(wave, "f_idx")) + 1)
-            v_d = _c128_f(_get(wave, "v_d"))
-            mixes_in = list(_get(wave, "mixes"))
-            keep += [f_idx, v_d]
-            wv[w].n_f = len(f_idx)
-            wv[w].indices_f_to_unique = f_idx.ctypes.data_as(C.POINTER(C.c_int32))
-            wv[w].v_d = v_d.ctypes.data
-            wv[w].n_mixes = len(mixes_in)
-            wv[w].mixes = _mix_array(mixes_in, "response", keep)
-        d.n_measurements = len(waves)
-        d.waves = wv
-        d.device = int(device)
-        _check(lib.cui_born_plan_create_setup(C.byref(d), int(max_objects), C.byref(self._plan)))
+        d, keep = setup_desc(device=device, **setup)
+        self.loaded_from_cache = None
+        if cache_dir is None:
+            _check(lib.cui_born_plan_create_setup(C.byref(d), int(max_objects), C.byref(self._plan)))
+        else:
+            loaded = C.c_int32(0)
+            _check(lib.cui_born_plan_create_setup_cached(C.byref(d), int(max_objects), str(cache_dir).encode(),
+                                                         C.byref(self._plan), C.byref(loaded)))
+            self.loaded_from_cache = loaded.value
+        del keep
         self._finish(max_objects, device)
         return self
 
@@ -608,3 +576,71 @@ except ImportError:  # pragma: no cover
 def born_forward(gamma, op: OperatorBorn):
     """Differentiable forward apply (``torch.autograd``)."""
     return BornForward.apply(gamma, op)
+
+
+def setup_desc(*, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_start: float,
+               n_elements_axis: Sequence[int], pitch_axis: Sequence[float], width_axis: Sequence[float],
+               n_face_axis: Sequence[int], absorption: dict, f_unique, waves,
+               aa_tx_beta: Optional[float] = 0.5, aa_rx_beta: Optional[float] = 0.5, device: int = 0):
+    """``cui_born_setup_desc`` of a discretised setup and the arrays it points into (keep them
+    alive while the descriptor is used).
+
+    ``absorption``: ``{"kind": "none"|"time_causal", "c", "constant_db", "slope_db", "exponent",
+    "f_ref", "dispersion"}``.  ``waves``: objects or dicts with ``f_idx`` (0-based global
+    frequency indices), ``v_d`` ``(F_w, E)`` normal velocities and ``mixes`` (``f_idx``,
+    ``active``, ``response`` ``(F_mix, n_active)`` receive responses).  ``aa_*_beta=None``
+    switches an anti-aliasing filter off.
+    """
+    keep = []
+    d = SetupDesc()
+    nd = len(n_points_axis)
+    d.n_dims = nd
+    for k in range(nd):
+        d.n_points_axis[k] = int(n_points_axis[k])
+        d.delta_axis[k] = float(delta_axis[k])
+    for k in range(nd - 1):
+        d.n_elements_axis[k] = int(n_elements_axis[k])
+        d.pitch_axis[k] = float(pitch_axis[k])
+        d.width_axis[k] = float(width_axis[k])
+        d.n_face_axis[k] = int(n_face_axis[k])
+    d.z_start = float(z_start)
+    a = AbsorptionDesc()
+    a.kind = {"none": 0, "time_causal": 1}[absorption.get("kind", "none")]
+    a.c = float(absorption.get("c", 1500.0))
+    a.constant_db = float(absorption.get("constant_db", 0.0))
+    a.slope_db = float(absorption.get("slope_db", 0.0))
+    a.exponent = float(absorption.get("exponent", 1.0))
+    a.f_ref = float(absorption.get("f_ref", 4e6))
+    a.dispersion = int(bool(absorption.get("dispersion", True)))
+    d.absorption = a
+    d.aa_tx_beta = -1.0 if aa_tx_beta is None else float(aa_tx_beta)
+    d.aa_rx_beta = -1.0 if aa_rx_beta is None else float(aa_rx_beta)
+    f = np.ascontiguousarray(np.asarray(f_unique, dtype=np.float64))
+    keep.append(f)
+    d.n_f_unique = len(f)
+    d.f_unique = f.ctypes.data_as(C.POINTER(C.c_double))
+    wv = (WaveDesc * len(waves))()
+    for w, wave in enumerate(waves):
+        f_idx = _i32(np.asarray(_get(wave, "f_idx")) + 1)
+        v_d = _c128_f(_get(wave, "v_d"))
+        mixes_in = list(_get(wave, "mixes"))
+        keep += [f_idx, v_d]
+        wv[w].n_f = len(f_idx)
+        wv[w].indices_f_to_unique = f_idx.ctypes.data_as(C.POINTER(C.c_int32))
+        wv[w].v_d = v_d.ctypes.data
+        wv[w].n_mixes = len(mixes_in)
+        wv[w].mixes = _mix_array(mixes_in, "response", keep)
+    d.n_measurements = len(waves)
+    d.waves = wv
+    keep.append(wv)
+    d.device = int(device)
+    return d, keep
+
+
+def setup_hash(**setup) -> str:
+    """Hash of the setup fields the device tables depend on (``cui_born_setup_hash``): the
+    16-hex-digit name part of the table-cache file.  Needs no GPU."""
+    d, keep = setup_desc(**setup)
+    out = C.create_string_buffer(17)
+    _check(load_library().cui_born_setup_hash(C.byref(d), out))
+    return out.value.decode()

@@ -159,6 +159,13 @@ cui_status build_metadata(Plan& p, const std::vector<MeasIn>& ms, const std::vec
 cui_status select_device_and_shapes(Plan& p, int device);
 cui_status upload_metadata_and_workspace(Plan& p);
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes);
+// table cache (cui_cache.cu): canonical key of the setup fields the device tables depend on,
+// its file path under `dir`, and loading / storing p.table and p.p_in
+cui_status setup_key(const cui_born_setup_desc* d, std::vector<unsigned char>& key);
+uint64_t key_hash(const std::vector<unsigned char>& key);
+std::string cache_path(const char* dir, const std::vector<unsigned char>& key);
+cui_status cache_load(const std::string& path, const std::vector<unsigned char>& key, Plan& p, bool* hit);
+cui_status cache_store(const std::string& path, const std::vector<unsigned char>& key, const Plan& p);
 
 // apply entry points used by the host wrappers ----------------------------
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu,

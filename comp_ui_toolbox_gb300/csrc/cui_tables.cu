@@ -275,7 +275,8 @@ cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk
     return CUI_OK;
 }
 
-cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan& p) {
+cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan& p, const char* cache_dir,
+                        int32_t* loaded) {
     if (!d) return set_error(CUI_ERR_INVALID_ARG, "desc is NULL");
     if (d->n_dims != 2 && d->n_dims != 3) return set_error(CUI_ERR_INVALID_ARG, "n_dims must be 2 or 3");
     const int nl = d->n_dims - 1;
@@ -346,6 +347,19 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
         return st;
     p.table_bytes = tbytes;
     p.incident_bytes = sizeof(float2) * static_cast<size_t>(p.S) * p.P;
+    // compute_or_load_hash.m:65-185: load both arrays from the cache file of this setup if it exists
+    std::vector<unsigned char> key;
+    std::string path;
+    if (cache_dir) {
+        if ((st = setup_key(d, key)) != CUI_OK) return st;
+        path = cache_path(cache_dir, key);
+        bool hit = false;
+        if ((st = cache_load(path, key, p, &hit)) != CUI_OK) return st;
+        if (hit) {
+            if (loaded) *loaded = 1;
+            return upload_metadata_and_workspace(p);
+        }
+    }
     const bool same_filter = (d->aa_tx_beta < 0.0 && d->aa_rx_beta < 0.0) || (d->aa_tx_beta == d->aa_rx_beta);
     if ((ce = talloc(reinterpret_cast<void**>(&dk), sizeof(double2) * p.F)) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dvd), sizeof(float2) * vd.size())) != cudaSuccess ||
@@ -388,6 +402,10 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
     }
     release();
     if (st != CUI_OK) return st;
+    if (cache_dir) {  // a failed store keeps the plan: *loaded = -1, the reason in cui_last_error()
+        const cui_status cs = cache_store(path, key, p);
+        if (loaded) *loaded = cs == CUI_OK ? 0 : -1;
+    }
     return upload_metadata_and_workspace(p);
 }
 #undef CUI_TRY
@@ -395,15 +413,16 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
 }  // namespace
 }  // namespace cui
 
-extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
-                                                 cui_born_plan** plan) {
+namespace {
+cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_objects, const char* cache_dir,
+                             int32_t* loaded, cui_born_plan** plan) {
     if (!plan) return cui::set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     *plan = nullptr;
     cui_born_plan* h = new (std::nothrow) cui_born_plan();
     if (!h) return cui::set_error(CUI_ERR_OOM, "host allocation failed");
     cui_status s;
     try {
-        s = cui::create_setup(desc, max_objects, h->p);
+        s = cui::create_setup(desc, max_objects, h->p, cache_dir, loaded);
     } catch (const std::bad_alloc&) {
         s = cui::set_error(CUI_ERR_OOM, "host allocation failed");
     }
@@ -413,4 +432,17 @@ extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc
     }
     *plan = h;
     return CUI_OK;
+}
+}  // namespace
+
+extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
+                                                 cui_born_plan** plan) {
+    return create_setup_plan(desc, max_objects, nullptr, nullptr, plan);
+}
+
+extern "C" cui_status cui_born_plan_create_setup_cached(const cui_born_setup_desc* desc, int32_t max_objects,
+                                                        const char* cache_dir, cui_born_plan** plan, int32_t* loaded) {
+    if (!cache_dir) return cui::set_error(CUI_ERR_INVALID_ARG, "cache_dir is NULL");
+    if (loaded) *loaded = 0;
+    return create_setup_plan(desc, max_objects, cache_dir, loaded, plan);
 }

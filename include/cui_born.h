@@ -172,6 +172,22 @@ typedef struct {
 cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, cui_born_plan** plan);
 /* Same plan from the setup form (tables computed on the device). */
 cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects, cui_born_plan** plan);
+/* Same, through an on-disk cache of the two device-built arrays (the lateral
+ * table and the incident fields), keyed like compute_or_load_hash
+ * (+auxiliary/compute_or_load_hash.m:65-185): the file
+ * `cache_dir`/cui_born_<cui_born_setup_hash>.tables is loaded when it exists,
+ * else the arrays are computed and stored there (written to a temporary name,
+ * then renamed).  A file whose stored setup differs from `desc` is a hash
+ * collision: CUI_ERR_INVALID_ARG, as in the reference (:90-107).  `*loaded`
+ * (may be NULL) = 1 loaded, 0 computed and stored, -1 computed but not stored
+ * (the plan is still returned; cui_last_error() says why). */
+cui_status cui_born_plan_create_setup_cached(const cui_born_setup_desc* desc, int32_t max_objects,
+                                             const char* cache_dir, cui_born_plan** plan, int32_t* loaded);
+/* Hash of the setup fields the device tables depend on -- grid, array, faces,
+ * medium, anti-aliasing, frequencies, each wave's frequency map and normal
+ * velocities; not the receive mixes or the device -- as 16 hex digits and a
+ * NUL in `hex17`.  Host only (no GPU). */
+cui_status cui_born_setup_hash(const cui_born_setup_desc* desc, char* hex17);
 cui_status cui_born_plan_destroy(cui_born_plan* plan);
 cui_status cui_born_plan_info(const cui_born_plan* plan, cui_born_info* info);
 
