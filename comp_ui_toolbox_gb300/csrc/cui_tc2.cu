@@ -158,7 +158,9 @@ struct FwdCfg {
     static constexpr int NR = 4;                 // raw stages
     static constexpr int STB = NT * 1024;        // 4NT rows x 64 points x 4 B
     static constexpr int SBO = 2048;             // 8-row groups: 16 K groups x 128 B
-    static constexpr uint32_t TCOLS = 8 * NT;    // 2 accumulators x 4NT columns
+    // accumulators of 4NT columns; 16-column blocks run two per SM and take half of tensor memory each
+    static constexpr uint32_t TCOLS = NT >= 32 ? 512 : 256;
+    static constexpr int NACC = TCOLS / (4 * NT);
     static constexpr int ITEMS = NT / 16;        // (4 points, column) items per producer
     static constexpr int LAG = NS - 1;           // read-out trails staging by LAG stages
 };
@@ -173,7 +175,7 @@ struct FwdLayout {
         oRaw = C::NS * C::STB;
         oBand = oRaw + C::NR * RS;
         oBar = oBand + 16 * RBW;
-        total = static_cast<size_t>(oBar) + 8 * (2 * C::NS + 2 * C::NR + 9) + 16;
+        total = static_cast<size_t>(oBar) + 8 * (2 * C::NS + 2 * C::NR + 2 * C::NACC + 5) + 16;
     }
 };
 
@@ -201,8 +203,9 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
     const uint32_t sRaw = sB + L.oRaw, sBand = sB + L.oBand;
     const uint32_t bar0 = sB + L.oBar;
     const uint32_t FULL = bar0, EMPTY = bar0 + 8 * C::NS, RAWF = bar0 + 16 * C::NS, RAWE = RAWF + 8 * C::NR,
-                   ACCF = RAWF + 16 * C::NR, ACCE = ACCF + 16, BANDF = ACCF + 32, BANDE = ACCF + 48, DRAIN = ACCF + 64;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NS + 2 * C::NR + 9));
+                   ACCF = RAWF + 16 * C::NR, ACCE = ACCF + 8 * C::NACC, BANDF = ACCE + 8 * C::NACC, BANDE = BANDF + 16,
+                   DRAIN = BANDF + 32;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NS + 2 * C::NR + 2 * C::NACC + 5));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
     if (tid == 0) {
@@ -214,9 +217,11 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             tc::bar_init(RAWF + 8 * s, 1);
             tc::bar_init(RAWE + 8 * s, kProd);
         }
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < C::NACC; ++k) {
             tc::bar_init(ACCF + 8 * k, 1);
             tc::bar_init(ACCE + 8 * k, kProd);
+        }
+        for (int k = 0; k < 2; ++k) {
             tc::bar_init(BANDF + 8 * k, 1);
             tc::bar_init(BANDE + 8 * k, 1);
         }
@@ -248,10 +253,10 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                     break;
                 const int s = q % C::NS;
                 if (!(ok = tc::bar_wait_abortable(FULL + 8 * s, (q / C::NS) & 1, abort_flag, kWaitLimitNs))) break;
-                const int k = q / kChainChunks, acc = k & 1;
+                const int k = q / kChainChunks, acc = static_cast<int>(static_cast<unsigned>(k) % C::NACC);
                 const bool first = (q % kChainChunks) == 0;
-                if (first && k >= 2 &&
-                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((k >> 1) - 1) & 1, abort_flag, kWaitLimitNs)))
+                if (first && k >= C::NACC &&
+                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(k) / C::NACC) - 1) & 1, abort_flag, kWaitLimitNs)))
                     break;
                 tc::fence_after_sync();
                 const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
@@ -402,8 +407,8 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             }
             const int qr = q - C::LAG;
             if (qr >= 0 && (qr % kChainChunks == kChainChunks - 1 || qr == Q - 1)) {
-                const int k = qr / kChainChunks, accs = k & 1;
-                if (!(ok = warp_wait(ACCF + 8 * accs, (k >> 1) & 1, abort_flag))) break;
+                const int k = qr / kChainChunks, accs = static_cast<int>(static_cast<unsigned>(k) % C::NACC);
+                if (!(ok = warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(k) / C::NACC) & 1, abort_flag))) break;
                 tc::fence_after_sync();
                 const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NT);
 #pragma unroll
@@ -516,8 +521,12 @@ struct AdjCfg {
     static constexpr int NB = NT >= 64 ? 1 : 2;  // V tile buffers (128 KB each at 64 columns)
     static constexpr int NA = 3;                 // spread-chunk stages
     static constexpr int NP = 3;                 // incident-field stages
-    static constexpr uint32_t TCOLS = 8 * NT;    // 2 accumulators x 4NT columns
-    static constexpr int LAG = 2;                // the epilogue trails the spreading by 2 units
+    static constexpr int NACC = 512 / (4 * NT);  // accumulators of 4NT columns: all of tensor memory
+    static constexpr uint32_t TCOLS = 512;
+    static constexpr int LAG = 2;                // shared roles: the epilogue trails the spreading by 2 units
+    // 16/32-column tiles: warps 0-3 spread the A operand and warps 4-7 run the epilogues, each
+    // group at its own pace (the epilogue of a unit may trail its MMAs by up to NACC units)
+    static constexpr bool SPLIT = NT <= 32;
     static constexpr int MAXL = 2;               // grid lines per block
 };
 
@@ -536,7 +545,7 @@ struct AdjLayout {  // byte offsets of the dynamic shared memory
         oBand = oP + C::NP * PS;
         oF = oBand + 16 * RBW;
         oBar = (oF + 4 * fchunk + 7) & ~7;
-        total = static_cast<size_t>(oBar) + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 9) + 16;
+        total = static_cast<size_t>(oBar) + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 2 * C::NACC + 5) + 16;
     }
 };
 
@@ -560,9 +569,10 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
     int* sF = reinterpret_cast<int*>(smem + L.oF);
     const uint32_t bar0 = sbase + L.oBar;
     const uint32_t BFULL = bar0, BEMPTY = BFULL + 8 * C::NB, AFULL = BEMPTY + 8 * C::NB, AEMPTY = AFULL + 8 * C::NA,
-                   PF = AEMPTY + 8 * C::NA, PE = PF + 8 * C::NP, ACCF = PE + 8 * C::NP, ACCE = ACCF + 16,
-                   BANDF = ACCF + 32, BANDE = ACCF + 48, DRAIN = ACCF + 64;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 9));
+                   PF = AEMPTY + 8 * C::NA, PE = PF + 8 * C::NP, ACCF = PE + 8 * C::NP, ACCE = ACCF + 8 * C::NACC,
+                   BANDF = ACCE + 8 * C::NACC, BANDE = BANDF + 16, DRAIN = BANDF + 32;
+    uint32_t* tslot =
+        reinterpret_cast<uint32_t*>(smem + L.oBar + 8 * (2 * C::NB + 2 * C::NA + 2 * C::NP + 2 * C::NACC + 5));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
     volatile int* nfa_s = reinterpret_cast<volatile int*>(tslot + 2);
 
@@ -571,19 +581,23 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             tc::bar_init(BFULL + 8 * k, 1);
             tc::bar_init(BEMPTY + 8 * k, 1);
         }
-        for (int k = 0; k < 2; ++k) {
+        // with split roles, 4 warps spread (AFULL, BANDE) and 4 run the epilogue (PE, ACCE)
+        const uint32_t n_role = C::SPLIT ? kProd / 2 : kProd;
+        for (int k = 0; k < C::NACC; ++k) {
             tc::bar_init(ACCF + 8 * k, 1);
-            tc::bar_init(ACCE + 8 * k, kProd);
+            tc::bar_init(ACCE + 8 * k, n_role);
+        }
+        for (int k = 0; k < 2; ++k) {
             tc::bar_init(BANDF + 8 * k, 1);
-            tc::bar_init(BANDE + 8 * k, kProd);
+            tc::bar_init(BANDE + 8 * k, n_role);
         }
         for (int s = 0; s < C::NA; ++s) {
-            tc::bar_init(AFULL + 8 * s, kProd);
+            tc::bar_init(AFULL + 8 * s, n_role);
             tc::bar_init(AEMPTY + 8 * s, 1);
         }
         for (int s = 0; s < C::NP; ++s) {
             tc::bar_init(PF + 8 * s, 1);
-            tc::bar_init(PE + 8 * s, kProd);
+            tc::bar_init(PE + 8 * s, n_role);
         }
         tc::bar_init(DRAIN, 1);
         *abort_flag = 0;
@@ -624,8 +638,9 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                     break;
                 const int sa = u % C::NA;
                 if (!(ok = tc::bar_wait_abortable(AFULL + 8 * sa, (u / C::NA) & 1, abort_flag, kWaitLimitNs))) break;
-                const int acc = u & 1;
-                if (u >= 2 && !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((u >> 1) - 1) & 1, abort_flag, kWaitLimitNs)))
+                const int acc = static_cast<int>(static_cast<unsigned>(u) % C::NACC);
+                if (u >= C::NACC &&
+                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(u) / C::NACC) - 1) & 1, abort_flag, kWaitLimitNs)))
                     break;
                 tc::fence_after_sync();
                 const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
@@ -714,9 +729,13 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
         const int qd = warp & 3, h = warp >> 2;
         const int j = qd * 32 + lane;
         const uint32_t lane_addr = static_cast<uint32_t>(qd * 32) << 16;
-        constexpr int NH = NT / 2;                      // columns of this half
-        constexpr int MW = NH < 16 ? NH : 16;           // columns per pass
+        // columns per epilogue thread: half of the tile with shared roles, all of it with split roles
+        constexpr int NH = C::SPLIT ? NT : NT / 2;
+        // columns per pass: at most 16 and within one object (tiles of 16 or 32 columns hold at most
+        // 2 objects, of 64 columns 4 objects of 16)
+        constexpr int MW = C::SPLIT ? NT / 2 : (NH < 16 ? NH : 16);
         constexpr int NPS = NH / MW;                    // passes; pass ps holds one object of the tile
+        const int hc = C::SPLIT ? 0 : h;                // column half of this thread's epilogue
         const int per = cols_per_object<NT>(a.Bt);
         float gx[C::MAXL][4][NPS], gy[C::MAXL][4][NPS];  // gamma_hat of x = r + 4j, line zi, pass object
 #pragma unroll
@@ -726,97 +745,109 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
 #pragma unroll
                 for (int ps = 0; ps < NPS; ++ps) gx[zz][rr][ps] = gy[zz][rr][ps] = 0.f;
         bool ok = true;
-        for (int it = 0; it < U + C::LAG && ok; ++it) {
-            if (it < U) {
-                const int fi = it / upf, rem = it - fi * upf, zi = rem >> 2, r = rem & 3, q = fi * nL + zi, bb = q & 1;
-                if (r == 0 && !(ok = warp_wait(BANDF + 8 * bb, (q >> 1) & 1, abort_flag))) break;
-                // ---- spread chunks of residue r -> A stage ----
-                const int sa = it % C::NA;
-                if (it >= C::NA && !(ok = warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag))) break;
-                const uint32_t as = sA + sa * L.AB;
-                for (int idx = tid; idx < 2 * NCH; idx += kProd) {
-                    const int v = idx >= NCH ? 1 : 0, i = idx - v * NCH;
-                    const uint32_t row = sBand + (bb * 2 + v) * a.RBW * 4u + 4u * (r + 4 * i);
-                    uint32_t w0, w1, w2, w3;
-                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w0) : "r"(row) : "memory");
-                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w1) : "r"(row + 16) : "memory");
-                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w2) : "r"(row + 32) : "memory");
-                    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w3) : "r"(row + 48) : "memory");
-                    sts128(as + 16u * idx, w0, w1, w2, w3);
-                }
-                tc::fence_async_smem();  // orders these generic accesses before the MMAs and the next row copy
-                tc::bar_arrive(AFULL + 8 * sa);
-                if (r == 3) tc::bar_arrive(BANDE + 8 * bb);
+        // ---- spread chunks of residue r of unit `it` -> A stage (threads t0 .. t0 + nthr - 1) ----
+        auto spread = [&](int it, int t0, int nthr) -> bool {
+            const int fi = it / upf, rem = it - fi * upf, zi = rem >> 2, r = rem & 3, q = fi * nL + zi, bb = q & 1;
+            if (r == 0 && !warp_wait(BANDF + 8 * bb, (q >> 1) & 1, abort_flag)) return false;
+            const int sa = it % C::NA;
+            if (it >= C::NA && !warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag)) return false;
+            const uint32_t as = sA + sa * L.AB;
+            for (int idx = tid - t0; idx < 2 * NCH; idx += nthr) {
+                const int v = idx >= NCH ? 1 : 0, i = idx - v * NCH;
+                const uint32_t row = sBand + (bb * 2 + v) * a.RBW * 4u + 4u * (r + 4 * i);
+                uint32_t w0, w1, w2, w3;
+                asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w0) : "r"(row) : "memory");
+                asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w1) : "r"(row + 16) : "memory");
+                asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w2) : "r"(row + 32) : "memory");
+                asm volatile("ld.shared.b32 %0, [%1];" : "=r"(w3) : "r"(row + 48) : "memory");
+                sts128(as + 16u * idx, w0, w1, w2, w3);
             }
-            // ---- epilogue of unit ue ----
-            const int ue = it - C::LAG;
-            if (ue >= 0) {
-                const int fi = ue / upf, rem = ue - fi * upf, zi = rem >> 2, r = rem & 3;
-                const int accs = ue & 1, pu = ue % C::NP;
-                const int f = sF[fi];
-                const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
-                const bool xin = r + 4 * j < a.Nx;
-                if (!(ok = warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag))) break;
-                float2 pv[NPS][MW];
+            tc::fence_async_smem();  // orders these generic accesses before the MMAs and the next row copy
+            tc::bar_arrive(AFULL + 8 * sa);
+            if (r == 3) tc::bar_arrive(BANDE + 8 * bb);
+            return true;
+        };
+        // ---- epilogue of unit ue: gamma_hat(x) += conj(p_in) * Z over this thread's columns ----
+        auto epilogue = [&](int ue) -> bool {
+            const int fi = ue / upf, rem = ue - fi * upf, zi = rem >> 2, r = rem & 3;
+            const int accs = static_cast<int>(static_cast<unsigned>(ue) % C::NACC), pu = ue % C::NP;
+            const int f = sF[fi];
+            const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
+            const bool xin = r + 4 * j < a.Nx;
+            if (!warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag)) return false;
+            float2 pv[NPS][MW];
 #pragma unroll
-                for (int ps = 0; ps < NPS; ++ps)
+            for (int ps = 0; ps < NPS; ++ps)
 #pragma unroll
-                    for (int m = 0; m < MW; ++m) {
-                        const int c = h * NH + ps * MW + m, bl = c / per, sl = c - bl * per;
-                        pv[ps][m] = make_float2(0.f, 0.f);  // unused columns contribute zero
-                        if (sl < ns && b0 + bl < a.B && xin)
-                            asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
-                                         : "=f"(pv[ps][m].x), "=f"(pv[ps][m].y)
-                                         : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
-                    }
-                tc::fence_async_smem();  // generic reads before the next bulk copy into this stage
-                tc::bar_arrive(PE + 8 * pu);
-                if (!(ok = warp_wait(ACCF + 8 * accs, (ue >> 1) & 1, abort_flag))) break;
-                tc::fence_after_sync();
-#pragma unroll
-                for (int ps = 0; ps < NPS; ++ps) {
-                    const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NH + ps * MW);
-                    float d0[MW], d1[MW], d2[MW], d3[MW];
-                    if constexpr (MW == 16) {
-                        tc::tmem_ld16(col, d0);
-                        tc::tmem_ld16(col + NT, d1);
-                        tc::tmem_ld16(col + 2 * NT, d2);
-                        tc::tmem_ld16(col + 3 * NT, d3);
-                    } else {
-                        tc::tmem_ld8(col, d0);
-                        tc::tmem_ld8(col + NT, d1);
-                        tc::tmem_ld8(col + 2 * NT, d2);
-                        tc::tmem_ld8(col + 3 * NT, d3);
-                    }
-                    tc::tmem_wait_ld();
-                    float sx = 0.f, sy = 0.f;
-#pragma unroll
-                    for (int m = 0; m < MW; ++m) {
-                        const float zr = d0[m] + d2[m], zi2 = -(d1[m] + d3[m]);
-                        const float px = pv[ps][m].x, py = pv[ps][m].y;
-                        sx = fmaf(px, zr, fmaf(py, zi2, sx));  // conj(p) * Z
-                        sy = fmaf(px, zi2, fmaf(-py, zr, sy));
-                    }
-#pragma unroll
-                    for (int zz = 0; zz < C::MAXL; ++zz)
-#pragma unroll
-                        for (int rr = 0; rr < 4; ++rr)
-                            if (zz == zi && rr == r) {
-                                gx[zz][rr][ps] += sx;
-                                gy[zz][rr][ps] += sy;
-                            }
+                for (int m = 0; m < MW; ++m) {
+                    const int c = hc * NH + ps * MW + m, bl = c / per, sl = c - bl * per;
+                    pv[ps][m] = make_float2(0.f, 0.f);  // unused columns contribute zero
+                    if (sl < ns && b0 + bl < a.B && xin)
+                        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                                     : "=f"(pv[ps][m].x), "=f"(pv[ps][m].y)
+                                     : "r"(sP + pu * L.PS + (sl * a.Jp + j) * 8) : "memory");
                 }
-                tc::fence_before_sync();
-                tc::bar_arrive(ACCE + 8 * accs);
+            tc::fence_async_smem();  // generic reads before the next bulk copy into this stage
+            tc::bar_arrive(PE + 8 * pu);
+            if (!warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(ue) / C::NACC) & 1, abort_flag)) return false;
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ps = 0; ps < NPS; ++ps) {
+                const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + hc * NH + ps * MW);
+                float d0[MW], d1[MW], d2[MW], d3[MW];
+                if constexpr (MW == 16) {
+                    tc::tmem_ld16(col, d0);
+                    tc::tmem_ld16(col + NT, d1);
+                    tc::tmem_ld16(col + 2 * NT, d2);
+                    tc::tmem_ld16(col + 3 * NT, d3);
+                } else {
+                    tc::tmem_ld8(col, d0);
+                    tc::tmem_ld8(col + NT, d1);
+                    tc::tmem_ld8(col + 2 * NT, d2);
+                    tc::tmem_ld8(col + 3 * NT, d3);
+                }
+                tc::tmem_wait_ld();
+                float sx = 0.f, sy = 0.f;
+#pragma unroll
+                for (int m = 0; m < MW; ++m) {
+                    const float zr = d0[m] + d2[m], zi2 = -(d1[m] + d3[m]);
+                    const float px = pv[ps][m].x, py = pv[ps][m].y;
+                    sx = fmaf(px, zr, fmaf(py, zi2, sx));  // conj(p) * Z
+                    sy = fmaf(px, zi2, fmaf(-py, zr, sy));
+                }
+#pragma unroll
+                for (int zz = 0; zz < C::MAXL; ++zz)
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+                        if (zz == zi && rr == r) {
+                            gx[zz][rr][ps] += sx;
+                            gy[zz][rr][ps] += sy;
+                        }
+            }
+            tc::fence_before_sync();
+            tc::bar_arrive(ACCE + 8 * accs);
+            return true;
+        };
+        if constexpr (C::SPLIT) {
+            if (h == 0) {
+                for (int it = 0; it < U && ok; ++it) ok = spread(it, 0, kProd / 2);
+            } else {
+                for (int ue = 0; ue < U && ok; ++ue) ok = epilogue(ue);
+            }
+        } else {
+            for (int it = 0; it < U + C::LAG && ok; ++it) {
+                if (it < U) ok = spread(it, 0, kProd);
+                if (ok && it >= C::LAG) ok = epilogue(it - C::LAG);
             }
         }
         if (!ok) atomicOr(a.status, 4);
         // every MMA has completed (the last epilogue waited on it): the V buffers now hold the
-        // partial gamma_hat of each (half, pass): sG[h*NPS + ps][zi][x]
+        // partial gamma_hat of each (column half, pass): sG[hc*NPS + ps][zi][x]
         producers_sync();
         float2* sG = reinterpret_cast<float2*>(smem);
         const bool good = !*abort_flag;
-        if (good) {
+        const bool has_epilogue = !C::SPLIT || h == 1;  // threads whose gx/gy hold sums
+        if (good && has_epilogue) {
 #pragma unroll
             for (int zz = 0; zz < C::MAXL; ++zz)
 #pragma unroll
@@ -825,7 +856,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                     for (int ps = 0; ps < NPS; ++ps) {
                         const int x = rr + 4 * j;
                         if (zz < nL && x < a.Nx)
-                            sG[((static_cast<size_t>(h) * NPS + ps) * a.L + zz) * a.Nx + x] =
+                            sG[((static_cast<size_t>(hc) * NPS + ps) * a.L + zz) * a.Nx + x] =
                                 make_float2(gx[zz][rr][ps], gy[zz][rr][ps]);
                     }
         }
@@ -835,7 +866,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             for (int idx = tid; idx < nb * nL * a.Nx; idx += kProd) {
                 const int bl = idx / (nL * a.Nx), rest = idx - bl * (nL * a.Nx), zz = rest / a.Nx, x = rest - zz * a.Nx;
                 float2 s = make_float2(0.f, 0.f);
-                for (int k = 0; k < 2 * NPS; ++k) {  // (half, pass) slots whose columns belong to object bl
+                for (int k = 0; k < (C::SPLIT ? 1 : 2) * NPS; ++k) {  // (half, pass) slots of object bl's columns
                     const int c0 = (k / NPS) * NH + (k % NPS) * MW;
                     if (c0 / per == bl) {
                         const float2 v = sG[(static_cast<size_t>(k) * a.L + zz) * a.Nx + x];
