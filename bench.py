@@ -51,6 +51,8 @@ def parse():
                     help="steps of the plain FP32 path timed after the main region (0: skip)")
     ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default="bf16x3",
                     help="adjoint contraction: FP32 CUDA cores or split-BF16 tcgen05 tensor cores")
+    ap.add_argument("--lasso-streams", type=int, default=4,
+                    help="2d-lasso: concurrent streams the problems are spread over inside the graph")
     ap.add_argument("--lasso-problems", type=int, default=16,
                     help="2d-lasso: how many of the 256 seeded problems go into the graph (device memory bound)")
     ap.add_argument("--lasso-iters", type=int, default=50)
@@ -394,7 +396,7 @@ def run_lasso(args):
     One step = one replay of the graph = ``--lasso-iters`` proximal-gradient
     iterations (forward, residual, adjoint, soft threshold) of each of the
     first ``--lasso-problems`` problems of the seeded batch; the problems run
-    concurrently on 4 streams inside the graph.  ``value`` counts one
+    concurrently on ``--lasso-streams`` streams inside the graph.  ``value`` counts one
     forward + adjoint apply per problem per iteration.
     """
     import numpy as np
@@ -428,7 +430,7 @@ def run_lasso(args):
         gs.append(torch.zeros((1, op.n_points), dtype=torch.complex64, device="cuda"))
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
-    streams = [torch.cuda.Stream() for _ in range(4)]
+    streams = [torch.cuda.Stream() for _ in range(max(1, args.lasso_streams))]
 
     tuned = []
     if args.precision == "auto":  # per-plan autotuner: the faster path for each problem

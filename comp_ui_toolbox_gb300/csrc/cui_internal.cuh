@@ -180,6 +180,9 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
 
 // shared-memory bytes the contraction kernels request
 size_t fwd_smem_bytes(const Plan* p, int nc);
+// element rows (ey) one FP32 forward block covers: the staged wave columns of a grid line feed
+// this many table rows (the 2D arrays have one)
+inline int fwd_rows_per_block(int Ey) { return Ey < 4 ? Ey : 4; }
 size_t adj_smem_bytes(const Plan* p, int nc);
 bool launch_shapes_ok(const Plan* p, std::string* why);
 // tensor-core path

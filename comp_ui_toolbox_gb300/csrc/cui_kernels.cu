@@ -85,6 +85,8 @@ struct FwdArgs {
     const int* __restrict__ f_slot_list;
     int lines_per_group, n_lines;
     int n_eg, nseg, Js, ntask;
+    int le;                     // lanes per element group; the 32/le lane groups split the j range
+    int eyb, n_eyb;             // element rows (ey) per block, blocks per line group
     int B, npass;
     float2* __restrict__ part;  // [groups][S][B][E]
 };
@@ -93,12 +95,15 @@ template <int NC, int KE>
 __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
-    float2* sA = reinterpret_cast<float2*>(smem_f4);
-    float2* sQ = sA + g.ppx * g.Ni;          // [Nx][NC]
-    float2* sR = sQ + g.Nx * NC;             // [Ex][NC]
+    const int EB = a.eyb;
+    float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of the block's element rows
+    float2* sQ = sA + EB * g.ppx * g.Ni;             // [Nx][NC]
+    float2* sR = sQ + g.Nx * NC;                     // [EB][Ex][NC]
     __shared__ int sSlot[NC];
 
-    const int grp = blockIdx.x / g.Ey, ey = blockIdx.x - grp * g.Ey;
+    // a block covers EB element rows ey0 .. ey0+EB-1: each staged q line feeds all of them
+    const int grp = blockIdx.x / a.n_eyb, ey0 = (blockIdx.x - grp * a.n_eyb) * EB;
+    const int neb = min(EB, g.Ey - ey0);
     const int f = blockIdx.y;
     const int b = blockIdx.z / a.npass, cp = blockIdx.z - b * a.npass;
     const int s0 = a.f_slot_ptr[f];
@@ -109,17 +114,24 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
     if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool task_on = warp < a.ntask;
-    int r = 0, eg = 0, seg = 0;
-    if (task_on) {
+    int r = 0, eg = 0, ek = 0, seg = 0;
+    if (warp < a.ntask) {
         r = warp % g.ppx;
-        const int rest = warp / g.ppx;
+        int rest = warp / g.ppx;
         eg = rest % a.n_eg;
-        seg = rest / a.n_eg;
+        rest /= a.n_eg;
+        ek = rest % EB;
+        seg = rest / EB;
     }
-    const int e0 = (eg * 32 + lane) * KE;
+    const bool task_on = warp < a.ntask && ek < neb;
+    // lane = (element group el, j sub-range sub): rows narrower than 32 windows of KE elements
+    // keep every lane busy by splitting the task's j range among 32/le lane groups
+    const int el = lane % a.le, sub = lane / a.le, nsub = 32 / a.le;
+    const int e0 = (eg * a.le + el) * KE;
     const int Nj_r = (r < g.Nx) ? (g.Nx - r + g.ppx - 1) / g.ppx : 0;
-    const int jlo = seg * a.Js, jhi = min(jlo + a.Js, Nj_r);
+    const int jlo0 = seg * a.Js, jhi0 = min(jlo0 + a.Js, Nj_r);
+    const int jspan = (max(jhi0 - jlo0, 0) + nsub - 1) / nsub;
+    const int jlo = jlo0 + sub * jspan, jhi = min(jlo + jspan, jhi0);
     const bool lane_on = task_on && (e0 < g.Ex) && (jlo < jhi);
 
     float2 acc[KE][NC];
@@ -132,11 +144,12 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
     const int line1 = min(line0 + a.lines_per_group, a.n_lines);
     for (int line = line0; line < line1; ++line) {
         const int iy = line % g.Ny, z = line / g.Ny;
-        const int oy = iy - ey * g.ppy + (g.Ey - 1) * g.ppy;
-        const float2* trow = a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox;
         const int64_t pt0 = (static_cast<int64_t>(z) * g.Ny + iy) * g.Nx;
         __syncthreads();
-        stage_band(sA, trow, g);
+        for (int k = 0; k < neb; ++k) {
+            const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
+            stage_band(sA + k * g.ppx * g.Ni, a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox, g);
+        }
         const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg + pt0;
         for (int idx = threadIdx.x; idx < NC * g.Nx; idx += blockDim.x) {
             const int c = idx / g.Nx, x = idx - c * g.Nx;
@@ -146,7 +159,7 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
         }
         __syncthreads();
         if (lane_on) {
-            const float2* Ar = sA + r * g.Ni + kPad;
+            const float2* Ar = sA + ek * g.ppx * g.Ni + r * g.Ni + kPad;
             int base = jlo - e0 + g.Ex - 1;
             float2 win[KE];
 #pragma unroll
@@ -170,30 +183,36 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
 
     // deterministic reduction over (residue, segment) tasks of the block
     __syncthreads();
-    for (int idx = threadIdx.x; idx < g.Ex * NC; idx += blockDim.x) sR[idx] = make_float2(0.f, 0.f);
+    for (int idx = threadIdx.x; idx < EB * g.Ex * NC; idx += blockDim.x) sR[idx] = make_float2(0.f, 0.f);
     __syncthreads();
     for (int w = 0; w < a.ntask; ++w) {
-        if (warp == w && lane_on) {
+        if (warp == w) {
+            for (int sb = 0; sb < nsub; ++sb) {  // lane groups of one warp add to the same elements in turn
+                if (sub == sb && lane_on) {
 #pragma unroll
-            for (int t = 0; t < KE; ++t) {
-                const int e = e0 + t;
-                if (e < g.Ex) {
+                    for (int t = 0; t < KE; ++t) {
+                        const int e = e0 + t;
+                        if (e < g.Ex) {
 #pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        float2 v = sR[e * NC + c];
-                        v.x += acc[t][c].x;
-                        v.y += acc[t][c].y;
-                        sR[e * NC + c] = v;
+                            for (int c = 0; c < NC; ++c) {
+                                float2 v = sR[(ek * g.Ex + e) * NC + c];
+                                v.x += acc[t][c].x;
+                                v.y += acc[t][c].y;
+                                sR[(ek * g.Ex + e) * NC + c] = v;
+                            }
+                        }
                     }
                 }
+                __syncwarp();
             }
         }
         __syncthreads();
     }
-    for (int idx = threadIdx.x; idx < nc * g.Ex; idx += blockDim.x) {
-        const int c = idx / g.Ex, ex = idx - c * g.Ex;
-        const int64_t o = ((static_cast<int64_t>(grp) * g.S + sSlot[c]) * a.B + b) * g.E + ex + g.Ex * ey;
-        a.part[o] = sR[ex * NC + c];
+    for (int idx = threadIdx.x; idx < neb * nc * g.Ex; idx += blockDim.x) {
+        const int k = idx / (nc * g.Ex), rem = idx - k * (nc * g.Ex);
+        const int c = rem / g.Ex, ex = rem - c * g.Ex;
+        const int64_t o = ((static_cast<int64_t>(grp) * g.S + sSlot[c]) * a.B + b) * g.E + ex + g.Ex * (ey0 + k);
+        a.part[o] = sR[(k * g.Ex + ex) * NC + c];
     }
 }
 
@@ -300,7 +319,9 @@ struct AdjArgs {
     const int* __restrict__ f_slot_list;
     int fchunk;
     int n_jg, nseg_e, Es, ntask;
+    int lj, nsub;                   // lanes per j group; lane groups splitting the element range
     int B;
+    int eyb;                        // element rows (ey) staged per synchronisation
     float2* __restrict__ part;      // [nfc][B][P]
 };
 
@@ -308,9 +329,10 @@ template <int NC, int KJ>
 __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
-    float2* sA = reinterpret_cast<float2*>(smem_f4);
-    float2* sV = sA + g.ppx * g.Ni;   // [Ex][NC]
-    float2* sR = sV + g.Ex * NC;      // [Nx]
+    const int EB = a.eyb;
+    float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of EB element rows
+    float2* sV = sA + EB * g.ppx * g.Ni;             // [EB][Ex][NC]
+    float2* sR = sV + EB * g.Ex * NC;                // [Nx]
     __shared__ int sSlot[NC];
 
     const int line = blockIdx.x;
@@ -327,10 +349,14 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
         jg = rest % a.n_jg;
         es = rest / a.n_jg;
     }
-    const int j0 = (jg * 32 + lane) * KJ;
+    // lane = (j group jl, element sub-range sub); lanes >= lj * nsub stay idle
+    const int jl = lane % a.lj, sub = lane / a.lj;
+    const int j0 = (jg * a.lj + jl) * KJ;
     const int Nj_r = (r < g.Nx) ? (g.Nx - r + g.ppx - 1) / g.ppx : 0;
-    const int elo = es * a.Es, ehi = min(elo + a.Es, g.Ex);
-    const bool lane_on = task_on && (j0 < Nj_r) && (elo < ehi);
+    const int elo0 = es * a.Es, ehi0 = min(elo0 + a.Es, g.Ex);
+    const int espan = (max(ehi0 - elo0, 0) + a.nsub - 1) / a.nsub;
+    const int elo = elo0 + sub * espan, ehi = min(elo + espan, ehi0);
+    const bool lane_on = task_on && sub < a.nsub && (j0 < Nj_r) && (elo < ehi);
 
     float2 gacc[KJ];
 #pragma unroll
@@ -347,39 +373,47 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
             for (int t = 0; t < KJ; ++t)
 #pragma unroll
                 for (int c = 0; c < NC; ++c) Z[t][c] = make_float2(0.f, 0.f);
-            for (int ey = 0; ey < g.Ey; ++ey) {
-                const int oy = iy - ey * g.ppy + (g.Ey - 1) * g.ppy;
-                const float2* trow = a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox;
+            // EB element rows per synchronisation: their table rows and V entries are staged together
+            for (int ey0 = 0; ey0 < g.Ey; ey0 += EB) {
+                const int neb = min(EB, g.Ey - ey0);
                 __syncthreads();
                 if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
-                stage_band(sA, trow, g);
+                for (int k = 0; k < neb; ++k) {
+                    const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
+                    stage_band(sA + k * g.ppx * g.Ni, a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox,
+                               g);
+                }
                 __syncthreads();
-                for (int idx = threadIdx.x; idx < NC * g.Ex; idx += blockDim.x) {
-                    const int c = idx / g.Ex, ex = idx - c * g.Ex;
-                    sV[ex * NC + c] = (c < nc)
-                        ? __ldg(a.V + (static_cast<int64_t>(sSlot[c]) * a.B + b) * g.E + ex + g.Ex * ey)
+                for (int idx = threadIdx.x; idx < neb * NC * g.Ex; idx += blockDim.x) {
+                    const int k = idx / (NC * g.Ex), rem = idx - k * (NC * g.Ex);
+                    const int c = rem / g.Ex, ex = rem - c * g.Ex;
+                    sV[(k * g.Ex + ex) * NC + c] = (c < nc)
+                        ? __ldg(a.V + (static_cast<int64_t>(sSlot[c]) * a.B + b) * g.E + ex + g.Ex * (ey0 + k))
                         : make_float2(0.f, 0.f);
                 }
                 __syncthreads();
                 if (lane_on) {
-                    const float2* Ar = sA + r * g.Ni + kPad;
-                    int base = j0 - elo + g.Ex - 1;
-                    float2 win[KJ];
+                    for (int k = 0; k < neb; ++k) {
+                        const float2* Ar = sA + k * g.ppx * g.Ni + r * g.Ni + kPad;
+                        const float2* sVk = sV + k * g.Ex * NC;
+                        int base = j0 - elo + g.Ex - 1;
+                        float2 win[KJ];
 #pragma unroll
-                    for (int t = 0; t < KJ; ++t) win[t] = Ar[base + t];
-                    for (int e = elo; e < ehi; ++e) {
-                        const float2* vx = sV + e * NC;
-                        float2 v[NC];
+                        for (int t = 0; t < KJ; ++t) win[t] = Ar[base + t];
+                        for (int e = elo; e < ehi; ++e) {
+                            const float2* vx = sVk + e * NC;
+                            float2 v[NC];
 #pragma unroll
-                        for (int c = 0; c < NC; ++c) v[c] = vx[c];
+                            for (int c = 0; c < NC; ++c) v[c] = vx[c];
 #pragma unroll
-                        for (int t = 0; t < KJ; ++t)
+                            for (int t = 0; t < KJ; ++t)
 #pragma unroll
-                            for (int c = 0; c < NC; ++c) cmac_conj(Z[t][c], win[t], v[c]);
+                                for (int c = 0; c < NC; ++c) cmac_conj(Z[t][c], win[t], v[c]);
 #pragma unroll
-                        for (int t = KJ - 1; t > 0; --t) win[t] = win[t - 1];
-                        --base;
-                        win[0] = Ar[base];
+                            for (int t = KJ - 1; t > 0; --t) win[t] = win[t - 1];
+                            --base;
+                            win[0] = Ar[base];
+                        }
                     }
                 }
             }
@@ -406,16 +440,21 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
     for (int idx = threadIdx.x; idx < g.Nx; idx += blockDim.x) sR[idx] = make_float2(0.f, 0.f);
     __syncthreads();
     for (int w = 0; w < a.ntask; ++w) {
-        if (warp == w && lane_on) {
+        if (warp == w) {
+            for (int sb = 0; sb < a.nsub; ++sb) {  // lane groups of one warp add to the same points in turn
+                if (sub == sb && lane_on) {
 #pragma unroll
-            for (int t = 0; t < KJ; ++t) {
-                const int x = r + g.ppx * (j0 + t);
-                if (x < g.Nx) {
-                    float2 v = sR[x];
-                    v.x += gacc[t].x;
-                    v.y += gacc[t].y;
-                    sR[x] = v;
+                    for (int t = 0; t < KJ; ++t) {
+                        const int x = r + g.ppx * (j0 + t);
+                        if (x < g.Nx) {
+                            float2 v = sR[x];
+                            v.x += gacc[t].x;
+                            v.y += gacc[t].y;
+                            sR[x] = v;
+                        }
+                    }
                 }
+                __syncwarp();
             }
         }
         __syncthreads();
@@ -516,10 +555,15 @@ LineGeom geom_of(const Plan* p) {
     return g;
 }
 
+// element rows (ey) whose table rows the FP32 adjoint stages together: all of them up to 8
+// (one synchronisation per 8 rows instead of three per row on the 3D matrix array)
+int adj_eyb(const Plan* p) { return std::min(p->Ey, 8); }
+
 int pick_nc(int slots) {
     if (slots <= 1) return 1;
     if (slots <= 2) return 2;
     if (slots <= 4) return 4;
+    if (slots <= 6) return 6;  // 5-6 waves (the 3D workload has 5): 8 would waste 3 of 8 columns
     if (slots <= 8) return 8;
     if (slots <= 12) return 12;
     return 16;
@@ -528,29 +572,32 @@ int pick_nc(int slots) {
 constexpr int fwd_ke(int nc) { return nc >= 16 ? 2 : 4; }
 constexpr int adj_kj(int nc) { return nc >= 12 ? 2 : 4; }
 
-// Register-window length per lane: the native length k0 when the warp's lanes
-// (32 x k per group) are mostly busy over n items (elements for the forward,
-// points of a residue for the adjoint), else a shorter one.  The 2D arrays
-// (128 elements, 128 points per residue) keep k0; the 3D matrix array's rows
-// (32 elements, 43 points per residue) would leave 3 of 4 lanes idle with k0 = 4.
-int pick_window(int n, int k0) {
+// Adjoint register-window length (points per lane) from k0 down to 1: the one that keeps most
+// of a warp's lanes and their window slots busy over the n points of a residue, where the lanes
+// form floor(32 / lj) groups of lj = ceil(n / k) lanes that split the element range (ties: the
+// longer window).  The 2D arrays (128 points per residue) keep k0 = 4; the 3D matrix array
+// (43 points per residue) takes 3: 2 groups of 15 lanes, 30 of 32 busy.
+int adj_window(int n, int k0) {
     auto util = [n](int k) {
-        const int per = 32 * k;
-        return static_cast<double>(n) / (static_cast<double>((n + per - 1) / per) * per);
+        const int lj = std::max(1, std::min(32, (n + k - 1) / k));
+        const int groups = (n + lj * k - 1) / (lj * k);
+        return static_cast<double>(n) / (static_cast<double>(groups) * lj * k) * (lj * (32 / lj)) / 32.0;
     };
     int best = k0;
-    for (int k : {2, 1})
-        if (k < k0 && util(k) > util(best) + 1e-9) best = k;
+    for (int k = k0 - 1; k >= 1; --k)
+        if (util(k) > util(best) + 1e-9) best = k;
     return best;
 }
 
-struct FwdShape { int n_eg, nseg, Js, ntask, threads; };
-struct AdjShape { int n_jg, nseg_e, Es, ntask, threads; };
+struct FwdShape { int le, n_eg, nseg, Js, ntask, threads; };
+struct AdjShape { int lj, nsub, n_jg, nseg_e, Es, ntask, threads; };
 
 FwdShape fwd_shape(const Plan* p, int ke) {
     FwdShape s;
-    s.n_eg = (p->Ex + 32 * ke - 1) / (32 * ke);
-    const int base = p->ppx * s.n_eg;
+    s.le = 32;  // lanes per element group: the smallest power of two >= Ex / ke, at most 32
+    while (s.le > 1 && (s.le / 2) * ke >= p->Ex) s.le /= 2;
+    s.n_eg = (p->Ex + s.le * ke - 1) / (s.le * ke);
+    const int base = p->ppx * s.n_eg * fwd_rows_per_block(p->Ey);
     s.nseg = std::max(1, 8 / base);
     s.nseg = std::min(s.nseg, std::max(1, p->Nj_max));
     s.Js = (p->Nj_max + s.nseg - 1) / s.nseg;
@@ -561,7 +608,9 @@ FwdShape fwd_shape(const Plan* p, int ke) {
 
 AdjShape adj_shape(const Plan* p, int kj) {
     AdjShape s;
-    s.n_jg = (p->Nj_max + 32 * kj - 1) / (32 * kj);
+    s.lj = std::max(1, std::min(32, (p->Nj_max + kj - 1) / kj));  // lanes per j group
+    s.nsub = 32 / s.lj;
+    s.n_jg = (p->Nj_max + s.lj * kj - 1) / (s.lj * kj);
     const int base = p->ppx * s.n_jg;
     s.nseg_e = std::max(1, 8 / base);
     s.nseg_e = std::min(s.nseg_e, p->Ex);
@@ -579,14 +628,15 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
     a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.lines_per_group = p->fwd_lines_per_group; a.n_lines = p->Ny * p->Nz;
-    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask;
+    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask; a.le = sh.le;
+    a.eyb = fwd_rows_per_block(p->Ey); a.n_eyb = (p->Ey + a.eyb - 1) / a.eyb;
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = p->ws_part;
     const size_t smem = fwd_smem_bytes(p, NC);
     cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    dim3 grid(p->fwd_groups * p->Ey, p->F, B * a.npass);
+    dim3 grid(p->fwd_groups * a.n_eyb, p->F, B * a.npass);
     if ((e = timing_begin(const_cast<Plan*>(p), 0, st)) != cudaSuccess) return e;
     fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
     count_launch();
@@ -603,7 +653,8 @@ cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.fchunk = p->adj_fchunk;
     a.n_jg = sh.n_jg; a.nseg_e = sh.nseg_e; a.Es = sh.Es; a.ntask = sh.ntask;
-    a.B = B; a.part = p->ws_part;
+    a.lj = sh.lj; a.nsub = sh.nsub;
+    a.B = B; a.eyb = adj_eyb(p); a.part = p->ws_part;
     const size_t smem = adj_smem_bytes(p, NC);
     cudaError_t e = cudaFuncSetAttribute(adj_dense_kernel<NC, KJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
@@ -616,22 +667,24 @@ cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
     return timing_end(const_cast<Plan*>(p), st);
 }
 
+// Forward window: the native one on rows of 32 x k0 elements or more; narrower rows (the 3D
+// matrix array's 32, the 64-element arrays) take 2 and split the j range among lane groups, since
+// the native window's registers would halve the resident blocks
+constexpr int fwd_window(int nc, int ex) { return (ex < 32 * fwd_ke(nc) && fwd_ke(nc) > 2) ? 2 : fwd_ke(nc); }
+
 template <int NC>
 cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
-    constexpr int K0 = fwd_ke(NC);
-    switch (pick_window(p->Ex, K0)) {
-        case 1: return launch_fwd_k<NC, 1>(p, gamma, ldg, B, st);
-        case 2: return launch_fwd_k<NC, (K0 > 2 ? 2 : K0)>(p, gamma, ldg, B, st);
-        default: return launch_fwd_k<NC, K0>(p, gamma, ldg, B, st);
-    }
+    if (fwd_window(NC, p->Ex) == 2) return launch_fwd_k<NC, 2>(p, gamma, ldg, B, st);
+    return launch_fwd_k<NC, fwd_ke(NC)>(p, gamma, ldg, B, st);
 }
 
 template <int NC>
 cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
     constexpr int K0 = adj_kj(NC);
-    switch (pick_window(p->Nj_max, K0)) {
+    switch (adj_window(p->Nj_max, K0)) {
         case 1: return launch_adj_k<NC, 1>(p, B, st);
         case 2: return launch_adj_k<NC, (K0 > 2 ? 2 : K0)>(p, B, st);
+        case 3: return launch_adj_k<NC, (K0 > 3 ? 3 : K0)>(p, B, st);
         default: return launch_adj_k<NC, K0>(p, B, st);
     }
 }
@@ -652,6 +705,7 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
         case 1: e = launch_fwd<1>(p, gamma, ldg, B, st); break;
         case 2: e = launch_fwd<2>(p, gamma, ldg, B, st); break;
         case 4: e = launch_fwd<4>(p, gamma, ldg, B, st); break;
+        case 6: e = launch_fwd<6>(p, gamma, ldg, B, st); break;
         case 8: e = launch_fwd<8>(p, gamma, ldg, B, st); break;
         case 12: e = launch_fwd<12>(p, gamma, ldg, B, st); break;
         default: e = launch_fwd<16>(p, gamma, ldg, B, st); break;
@@ -712,6 +766,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         case 1: e = launch_adj<1>(p, B, st); break;
         case 2: e = launch_adj<2>(p, B, st); break;
         case 4: e = launch_adj<4>(p, B, st); break;
+        case 6: e = launch_adj<6>(p, B, st); break;
         case 8: e = launch_adj<8>(p, B, st); break;
         case 12: e = launch_adj<12>(p, B, st); break;
         default: e = launch_adj<16>(p, B, st); break;
@@ -724,8 +779,8 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
 
 bool launch_shapes_ok(const Plan* p, std::string* why) {
     const int nc = pick_nc(p->max_slots_per_f);
-    const FwdShape f = fwd_shape(p, pick_window(p->Ex, nc >= 16 ? 2 : 4));
-    const AdjShape a = adj_shape(p, pick_window(p->Nj_max, nc >= 12 ? 2 : 4));
+    const FwdShape f = fwd_shape(p, fwd_window(nc, p->Ex));
+    const AdjShape a = adj_shape(p, adj_window(p->Nj_max, adj_kj(nc)));
     if (f.threads > 512 || a.threads > 512) {
         *why = "launch shape exceeds 512 threads (too many points per pitch or elements for this build)";
         return false;
@@ -761,13 +816,13 @@ void timing_release(Plan* p) {
 }
 
 size_t fwd_smem_bytes(const Plan* p, int nc) {
-    return sizeof(float2) * (static_cast<size_t>(p->ppx) * p->Ni + static_cast<size_t>(p->Nx) * nc +
-                             static_cast<size_t>(p->Ex) * nc);
+    const size_t eb = fwd_rows_per_block(p->Ey);
+    return sizeof(float2) * (eb * p->ppx * p->Ni + static_cast<size_t>(p->Nx) * nc + eb * p->Ex * nc);
 }
 
 size_t adj_smem_bytes(const Plan* p, int nc) {
-    return sizeof(float2) * (static_cast<size_t>(p->ppx) * p->Ni + static_cast<size_t>(p->Ex) * nc +
-                             static_cast<size_t>(p->Nx));
+    const size_t eb = adj_eyb(p);
+    return sizeof(float2) * (eb * p->ppx * p->Ni + eb * p->Ex * nc + static_cast<size_t>(p->Nx));
 }
 
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
@@ -866,14 +921,15 @@ cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, i
     a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.lines_per_group = lines_per_group; a.n_lines = p->Ny * p->Nz;
-    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask;
+    a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask; a.le = sh.le;
+    a.eyb = fwd_rows_per_block(p->Ey); a.n_eyb = (p->Ey + a.eyb - 1) / a.eyb;
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = part;
     const size_t smem = fwd_smem_bytes(p, NC);
     cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    dim3 grid(groups * p->Ey, p->F, B * a.npass);
+    dim3 grid(groups * a.n_eyb, p->F, B * a.npass);
     fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
@@ -911,6 +967,7 @@ extern "C" cui_status cui_born_forward_static(cui_born_plan* plan, const cui_com
         case 1: e = launch_fwd_static<1>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 2: e = launch_fwd_static<2>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 4: e = launch_fwd_static<4>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 6: e = launch_fwd_static<6>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 8: e = launch_fwd_static<8>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 12: e = launch_fwd_static<12>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         default: e = launch_fwd_static<16>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
