@@ -330,9 +330,12 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
     const int EB = a.eyb;
+    // V rows padded to an odd number of columns: lane groups reading elements espan apart then hit
+    // different banks
+    constexpr int NCP = NC | 1;
     float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of EB element rows
-    float2* sV = sA + EB * g.ppx * g.Ni;             // [EB][Ex][NC]
-    float2* sR = sV + EB * g.Ex * NC;                // [Nx]
+    float2* sV = sA + EB * g.ppx * g.Ni;             // [EB][Ex][NCP]
+    float2* sR = sV + EB * g.Ex * NCP;               // [Nx]
     __shared__ int sSlot[NC];
 
     const int line = blockIdx.x;
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
                 for (int idx = threadIdx.x; idx < neb * NC * g.Ex; idx += blockDim.x) {
                     const int k = idx / (NC * g.Ex), rem = idx - k * (NC * g.Ex);
                     const int c = rem / g.Ex, ex = rem - c * g.Ex;
-                    sV[(k * g.Ex + ex) * NC + c] = (c < nc)
+                    sV[(k * g.Ex + ex) * NCP + c] = (c < nc)
                         ? __ldg(a.V + (static_cast<int64_t>(sSlot[c]) * a.B + b) * g.E + ex + g.Ex * (ey0 + k))
                         : make_float2(0.f, 0.f);
                 }
@@ -395,13 +398,13 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
                 if (lane_on) {
                     for (int k = 0; k < neb; ++k) {
                         const float2* Ar = sA + k * g.ppx * g.Ni + r * g.Ni + kPad;
-                        const float2* sVk = sV + k * g.Ex * NC;
+                        const float2* sVk = sV + k * g.Ex * NCP;
                         int base = j0 - elo + g.Ex - 1;
                         float2 win[KJ];
 #pragma unroll
                         for (int t = 0; t < KJ; ++t) win[t] = Ar[base + t];
                         for (int e = elo; e < ehi; ++e) {
-                            const float2* vx = sVk + e * NC;
+                            const float2* vx = sVk + e * NCP;
                             float2 v[NC];
 #pragma unroll
                             for (int c = 0; c < NC; ++c) v[c] = vx[c];
@@ -822,7 +825,7 @@ size_t fwd_smem_bytes(const Plan* p, int nc) {
 
 size_t adj_smem_bytes(const Plan* p, int nc) {
     const size_t eb = adj_eyb(p);
-    return sizeof(float2) * (eb * p->ppx * p->Ni + eb * p->Ex * nc + static_cast<size_t>(p->Nx));
+    return sizeof(float2) * (eb * p->ppx * p->Ni + eb * p->Ex * (nc | 1) + static_cast<size_t>(p->Nx));
 }
 
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
