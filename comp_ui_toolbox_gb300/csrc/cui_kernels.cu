@@ -308,6 +308,143 @@ __global__ void unmix_kernel(const UnmixArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Slot-tiled mixing for batched applies (B >= 8 objects, E <= 256 elements).
+// Per slot s the mixing is a small complex product: u[rows of s][b] = P_s G[s]
+// with P_s[row][e] = pref[mix, f_row, pos(e)] (0 where e is not active), and
+// the unmixing its conjugate transpose V[s] = P_s^H u[rows of s].  A block
+// takes one slot and up to 32 objects: it stages G[s] (forward) or the slot's
+// rows of u (adjoint) and P_s in chunks of 32 rows in shared memory, lanes run
+// over objects, and every sum runs in a fixed order.
+// ---------------------------------------------------------------------------
+constexpr int kMixBC = 32;   // objects per block
+constexpr int kMixRC = 32;   // rows of P_s per chunk
+constexpr int kMixEMax = 256;
+
+struct MixTileArgs {
+    const int* __restrict__ slot_row_ptr;
+    const int* __restrict__ slot_rows;
+    const int* __restrict__ row_mix;
+    const int* __restrict__ row_fl;
+    const int* __restrict__ mix_nact;
+    const int* __restrict__ mix_nf;
+    const int* __restrict__ mix_act_off;
+    const int64_t* __restrict__ mix_pref_off;
+    const int* __restrict__ act;
+    const float2* __restrict__ pref;
+    int B, E;
+    const float2* __restrict__ G;  // forward input [S][B][E]
+    float2* __restrict__ u;        // forward output, column b at b * ldu
+    const float2* __restrict__ uin;  // adjoint input
+    int64_t ldu;
+    float2* __restrict__ V;        // adjoint output [S][B][E]
+};
+
+// P_s rows r0 .. r0+nk-1 of slot s into sP[k][e] (dense, zero-filled); sRow[k] = row index
+__device__ void stage_prefactors(const MixTileArgs& a, int rbeg, int r0, int nk, float2* sP, int* sRow) {
+    for (int i = threadIdx.x; i < nk * a.E; i += blockDim.x) sP[i] = make_float2(0.f, 0.f);
+    if (threadIdx.x < nk) sRow[threadIdx.x] = a.slot_rows[rbeg + r0 + threadIdx.x];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int k = warp; k < nk; k += nw) {
+        const int row = sRow[k], m = a.row_mix[row], fl = a.row_fl[row];
+        const int nact = a.mix_nact[m], nf = a.mix_nf[m];
+        const float2* pr = a.pref + a.mix_pref_off[m] + fl;
+        const int* ac = a.act + a.mix_act_off[m];
+        for (int ia = lane; ia < nact; ia += 32) sP[k * a.E + ac[ia]] = pr[static_cast<int64_t>(ia) * nf];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) mix_tile_kernel(const MixTileArgs a) {
+    extern __shared__ float4 smem_m4[];
+    float2* sG = reinterpret_cast<float2*>(smem_m4);         // [E][kMixBC + 1]
+    float2* sP = sG + a.E * (kMixBC + 1);                    // [kMixRC][E]
+    __shared__ int sRow[kMixRC];
+    const int s = blockIdx.x, b0 = blockIdx.y * kMixBC, nb = min(kMixBC, a.B - b0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x; i < nb * a.E; i += blockDim.x) {
+        const int bl = i / a.E, e = i - bl * a.E;
+        sG[e * (kMixBC + 1) + bl] = a.G[(static_cast<int64_t>(s) * a.B + b0 + bl) * a.E + e];
+    }
+    const int rbeg = a.slot_row_ptr[s], nrows = a.slot_row_ptr[s + 1] - rbeg;
+    for (int r0 = 0; r0 < nrows; r0 += kMixRC) {
+        const int nk = min(kMixRC, nrows - r0);
+        __syncthreads();  // previous chunk's readers are done (and sG is complete)
+        stage_prefactors(a, rbeg, r0, nk, sP, sRow);
+        for (int k = warp; k < nk; k += nw) {
+            const float2* pk = sP + k * a.E;
+            float2 acc = make_float2(0.f, 0.f);
+            for (int e = 0; e < a.E; ++e) cmac(acc, pk[e], sG[e * (kMixBC + 1) + lane]);
+            if (lane < nb) a.u[static_cast<int64_t>(b0 + lane) * a.ldu + sRow[k]] = acc;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) unmix_tile_kernel(const MixTileArgs a) {
+    extern __shared__ float4 smem_m4[];
+    float2* sP = reinterpret_cast<float2*>(smem_m4);          // [kMixRC][E]; at the end [kMixBC][E + 1]
+    float2* sU = sP + (kMixBC * (a.E + 1) > kMixRC * a.E ? kMixBC * (a.E + 1) : kMixRC * a.E);  // [kMixRC][kMixBC]
+    __shared__ int sRow[kMixRC];
+    const int s = blockIdx.x, b0 = blockIdx.y * kMixBC, nb = min(kMixBC, a.B - b0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    constexpr int EJ = kMixEMax / 8;  // elements per warp (8 warps)
+    float2 acc[EJ];
+#pragma unroll
+    for (int j = 0; j < EJ; ++j) acc[j] = make_float2(0.f, 0.f);
+    const int rbeg = a.slot_row_ptr[s], nrows = a.slot_row_ptr[s + 1] - rbeg;
+    for (int r0 = 0; r0 < nrows; r0 += kMixRC) {
+        const int nk = min(kMixRC, nrows - r0);
+        __syncthreads();
+        stage_prefactors(a, rbeg, r0, nk, sP, sRow);
+        for (int i = threadIdx.x; i < nk * kMixBC; i += blockDim.x) {
+            const int k = i / kMixBC, bl = i - k * kMixBC;
+            sU[i] = bl < nb ? a.uin[static_cast<int64_t>(b0 + bl) * a.ldu + sRow[k]] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        for (int k = 0; k < nk; ++k) {
+            const float2 uv = sU[k * kMixBC + lane];
+            const float2* pk = sP + k * a.E;
+#pragma unroll
+            for (int j = 0; j < EJ; ++j) {
+                const int e = warp + nw * j;
+                if (e < a.E) cmac_conj(acc[j], pk[e], uv);
+            }
+        }
+    }
+    // transpose through shared memory so that V is written along e
+    __syncthreads();
+    float2* sV = sP;  // [kMixBC][E + 1]
+#pragma unroll
+    for (int j = 0; j < EJ; ++j) {
+        const int e = warp + nw * j;
+        if (e < a.E) sV[lane * (a.E + 1) + e] = acc[j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb * a.E; i += blockDim.x) {
+        const int bl = i / a.E, e = i - bl * a.E;
+        a.V[(static_cast<int64_t>(s) * a.B + b0 + bl) * a.E + e] = sV[bl * (a.E + 1) + e];
+    }
+}
+
+size_t mix_tile_smem(int E) { return sizeof(float2) * (static_cast<size_t>(E) * (kMixBC + 1) + kMixRC * E); }
+size_t unmix_tile_smem(int E) {
+    return sizeof(float2) * (std::max<size_t>(static_cast<size_t>(kMixBC) * (E + 1), static_cast<size_t>(kMixRC) * E) +
+                             kMixRC * kMixBC);
+}
+
+MixTileArgs mix_tile_args(const Plan* p, int B) {
+    MixTileArgs m;
+    m.slot_row_ptr = p->slot_row_ptr; m.slot_rows = p->slot_rows; m.row_mix = p->row_mix; m.row_fl = p->row_fl;
+    m.mix_nact = p->mix_nact; m.mix_nf = p->mix_nf; m.mix_act_off = p->mix_act_off; m.mix_pref_off = p->mix_pref_off;
+    m.act = p->act; m.pref = p->pref; m.B = B; m.E = p->E;
+    m.G = nullptr; m.u = nullptr; m.uin = nullptr; m.ldu = 0; m.V = nullptr;
+    return m;
+}
+
+// the slot-tiled kernels serve batches of 8 or more objects on arrays of up to 256 elements
+bool use_mix_tile(const Plan* p, int B) { return B >= 8 && p->E <= kMixEMax; }
+
+// ---------------------------------------------------------------------------
 // dense adjoint: block = (grid line, frequency chunk, object)
 // ---------------------------------------------------------------------------
 struct AdjArgs {
@@ -718,6 +855,17 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (use_mix_tile(p, B)) {
+        MixTileArgs t = mix_tile_args(p, B);
+        t.G = p->ws_G; t.u = u; t.ldu = ldu;
+        const size_t smem = mix_tile_smem(p->E);
+        if ((e = cudaFuncSetAttribute(mix_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem))) != cudaSuccess)
+            return e;
+        mix_tile_kernel<<<dim3(p->S, (B + kMixBC - 1) / kMixBC), 256, smem, st>>>(t);
+        count_launch();
+        return cudaGetLastError();
+    }
     MixArgs m;
     m.G = p->ws_G; m.row_slot = p->row_slot; m.row_mix = p->row_mix; m.row_fl = p->row_fl;
     m.mix_nact = p->mix_nact; m.mix_nf = p->mix_nf; m.mix_pref_off = p->mix_pref_off; m.mix_act_off = p->mix_act_off;
@@ -747,14 +895,25 @@ cudaError_t finish_adjoint(Plan* p, int nfc, int B, float2* g, int64_t ldg, cons
 
 cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
                         const IstaArgs* ista = nullptr) {
-    UnmixArgs a;
-    a.u = u; a.ldu = ldu; a.slot_row_ptr = p->slot_row_ptr; a.slot_rows = p->slot_rows;
-    a.row_mix = p->row_mix; a.row_fl = p->row_fl; a.mix_nf = p->mix_nf; a.mix_pref_off = p->mix_pref_off;
-    a.pos = p->pos; a.pref = p->pref; a.S = p->S; a.B = B; a.E = p->E; a.V = p->ws_G;
-    const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
-    unmix_kernel<<<grid_1d(n, 256), 256, 0, st>>>(a);
+    cudaError_t e;
+    if (use_mix_tile(p, B)) {
+        MixTileArgs t = mix_tile_args(p, B);
+        t.uin = u; t.ldu = ldu; t.V = p->ws_G;
+        const size_t smem = unmix_tile_smem(p->E);
+        if ((e = cudaFuncSetAttribute(unmix_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem))) != cudaSuccess)
+            return e;
+        unmix_tile_kernel<<<dim3(p->S, (B + kMixBC - 1) / kMixBC), 256, smem, st>>>(t);
+    } else {
+        UnmixArgs a;
+        a.u = u; a.ldu = ldu; a.slot_row_ptr = p->slot_row_ptr; a.slot_rows = p->slot_rows;
+        a.row_mix = p->row_mix; a.row_fl = p->row_fl; a.mix_nf = p->mix_nf; a.mix_pref_off = p->mix_pref_off;
+        a.pos = p->pos; a.pref = p->pref; a.S = p->S; a.B = B; a.E = p->E; a.V = p->ws_G;
+        const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
+        unmix_kernel<<<grid_1d(n, 256), 256, 0, st>>>(a);
+    }
     count_launch();
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (p->precision == 1) {
         int nfc = p->adj_nfc;
