@@ -20,8 +20,8 @@
 // CoSaMP shares a)-c): the 2s largest proxy entries are 2s argmax passes that
 // mask each winner, the union's new columns come from the same column kernel,
 // and the least squares on the union is a Gram matrix (FP32 products, FP64
-// sums) solved by Cholesky on the host in FP64 with two steps of iterative
-// refinement against device residuals.  Pruning and the support bookkeeping
+// sums) solved by a pivoted Cholesky on the host in FP64 with two steps of
+// iterative refinement against device residuals.  Pruning and the support bookkeeping
 // (at most 3s integers) stay on the host.
 #include <cuda_runtime.h>
 
@@ -39,6 +39,8 @@ namespace {
 constexpr int kOmpThreads = 256;
 constexpr int kOmpBlocks = 256;  // partial sums / maxima per reduction (fixed: deterministic order)
 constexpr int kCosampMaxSparsity = 512;  // the host factorises Gram matrices of up to 3s x 3s
+// relative pivot below which a column counts as dependent: the Gram matrix sums FP32 products
+constexpr double kCosampPivotTol = 1e-6;
 
 // keep (v, i) if it beats (bv, bi): larger value, ties to the smaller index (MATLAB's max)
 __device__ __forceinline__ void keep_max(float& bv, int64_t& bi, float v, int64_t i) {
@@ -328,38 +330,70 @@ ColumnArgs column_args(const Plan& p) {
     return ca;
 }
 
-// In-place Cholesky G = L L^H of a Hermitian positive definite K x K matrix whose upper
-// triangle is stored row-major (G[i*K + j], i <= j); L^H overwrites the upper triangle.
-// Returns false when a pivot is not positive.
-bool cholesky_upper(std::vector<std::complex<double>>& G, int K) {
-    for (int j = 0; j < K; ++j) {
-        double d = G[static_cast<size_t>(j) * K + j].real();
-        for (int k = 0; k < j; ++k) d -= std::norm(G[static_cast<size_t>(k) * K + j]);
-        if (!(d > 0.0)) return false;
-        d = std::sqrt(d);
-        G[static_cast<size_t>(j) * K + j] = d;
-        for (int i = j + 1; i < K; ++i) {
-            std::complex<double> s = G[static_cast<size_t>(j) * K + i];
-            for (int k = 0; k < j; ++k) s -= std::conj(G[static_cast<size_t>(k) * K + j]) * G[static_cast<size_t>(k) * K + i];
-            G[static_cast<size_t>(j) * K + i] = s / d;
+// Least squares through the normal equations G c = b (G = A^H A, Hermitian positive
+// semidefinite, upper triangle given row-major), solved in FP64 by a Cholesky factorisation with
+// diagonal pivoting.  Pivots that fall below tol x the largest diagonal mark columns that are
+// linear combinations of the ones already taken (to the accuracy of a Gram matrix summed from
+// FP32 products); they are left out with coefficient 0, which is the basic solution a
+// column-pivoted QR -- MATLAB's A \ y of cosamp.m:244 -- gives for a rank-deficient A.
+struct PivotedCholesky {
+    int K = 0, r = 0;                      // size, numerical rank
+    std::vector<int> perm;                 // perm[j]: column taken as pivot j
+    std::vector<std::complex<double>> A;   // K x K: lower factor in columns 0..r-1
+
+    void factor(const std::vector<std::complex<double>>& Gup, int n, double tol) {
+        K = n;
+        r = 0;
+        perm.resize(K);
+        A.assign(static_cast<size_t>(K) * K, {});
+        double dmax = 0.0;
+        for (int i = 0; i < K; ++i) {
+            perm[i] = i;
+            for (int j = i; j < K; ++j) {
+                A[static_cast<size_t>(i) * K + j] = Gup[static_cast<size_t>(i) * K + j];
+                A[static_cast<size_t>(j) * K + i] = std::conj(Gup[static_cast<size_t>(i) * K + j]);
+            }
+            dmax = std::max(dmax, Gup[static_cast<size_t>(i) * K + i].real());
+        }
+        auto at = [&](int i, int j) -> std::complex<double>& { return A[static_cast<size_t>(i) * K + j]; };
+        for (int j = 0; j < K; ++j) {
+            int p = j;
+            for (int i = j + 1; i < K; ++i)
+                if (at(i, i).real() > at(p, p).real()) p = i;
+            if (!(at(p, p).real() > tol * dmax)) break;
+            if (p != j) {  // symmetric swap of rows and columns j and p
+                for (int c = 0; c < K; ++c) std::swap(at(j, c), at(p, c));
+                for (int c = 0; c < K; ++c) std::swap(at(c, j), at(c, p));
+                std::swap(perm[j], perm[p]);
+            }
+            const double l = std::sqrt(at(j, j).real());
+            at(j, j) = l;
+            for (int i = j + 1; i < K; ++i) at(i, j) /= l;
+            for (int i = j + 1; i < K; ++i)
+                for (int c = j + 1; c <= i; ++c) at(i, c) -= at(i, j) * std::conj(at(c, j));
+            for (int i = j + 1; i < K; ++i)  // keep the trailing block Hermitian for the next pivot search
+                for (int c = i + 1; c < K; ++c) at(i, c) = std::conj(at(c, i));
+            r = j + 1;
         }
     }
-    return true;
-}
 
-// x = (U^H U)^{-1} b with U the upper factor from cholesky_upper
-void cholesky_solve(const std::vector<std::complex<double>>& U, int K, std::vector<std::complex<double>>& x) {
-    for (int i = 0; i < K; ++i) {  // U^H z = b
-        std::complex<double> s = x[i];
-        for (int k = 0; k < i; ++k) s -= std::conj(U[static_cast<size_t>(k) * K + i]) * x[k];
-        x[i] = s / U[static_cast<size_t>(i) * K + i].real();
+    // x: right-hand side b on entry, coefficients c on return (0 for columns left out)
+    void solve(std::vector<std::complex<double>>& x) const {
+        std::vector<std::complex<double>> z(r);
+        for (int i = 0; i < r; ++i) {  // L z = P b
+            std::complex<double> v = x[perm[i]];
+            for (int k = 0; k < i; ++k) v -= A[static_cast<size_t>(i) * K + k] * z[k];
+            z[i] = v / A[static_cast<size_t>(i) * K + i].real();
+        }
+        for (int i = r - 1; i >= 0; --i) {  // L^H w = z
+            std::complex<double> v = z[i];
+            for (int k = i + 1; k < r; ++k) v -= std::conj(A[static_cast<size_t>(k) * K + i]) * z[k];
+            z[i] = v / A[static_cast<size_t>(i) * K + i].real();
+        }
+        std::fill(x.begin(), x.end(), std::complex<double>());
+        for (int i = 0; i < r; ++i) x[perm[i]] = z[i];
     }
-    for (int i = K - 1; i >= 0; --i) {  // U x = z
-        std::complex<double> s = x[i];
-        for (int k = i + 1; k < K; ++k) s -= U[static_cast<size_t>(i) * K + k] * x[k];
-        x[i] = s / U[static_cast<size_t>(i) * K + i].real();
-    }
-}
+};
 
 struct OmpWork {
     float2 *g, *Q, *a, *r, *part, *c, *d, *R, *qy, *rr;
@@ -683,11 +717,9 @@ extern "C" cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* 
                         U[static_cast<size_t>(i) * k + j] = {G_h[static_cast<size_t>(i) * K + j].x, G_h[static_cast<size_t>(i) * K + j].y};
                     c[i] = {G_h[static_cast<size_t>(i) * K + k].x, G_h[static_cast<size_t>(i) * K + k].y};
                 }
-                if (!cholesky_upper(U, k)) {
-                    status = set_error(CUI_ERR_NUMERIC, "cosamp: Gram matrix of the selected columns is not positive definite");
-                    break;
-                }
-                cholesky_solve(U, k, c);
+                PivotedCholesky pc;
+                pc.factor(U, k, kCosampPivotTol);
+                pc.solve(c);
                 // two steps of iterative refinement: c += (A^H A)^{-1} A^H (y - A c)
                 bool ok = true;
                 for (int ref = 0; ref < 2 && ok; ++ref) {
@@ -695,7 +727,7 @@ extern "C" cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* 
                     if (!ok) break;
                     std::vector<std::complex<double>> d(k);
                     for (int i = 0; i < k; ++i) d[i] = {d_h[i].x, d_h[i].y};
-                    cholesky_solve(U, k, d);
+                    pc.solve(d);
                     for (int i = 0; i < k; ++i) c[i] += d[i];
                 }
                 if (!ok) break;

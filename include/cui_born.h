@@ -281,8 +281,10 @@ cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, int32_t n_a
  * `atoms` and `coefficients` (s each: the final support in the reference's
  * order, largest coefficient first), `rel_residuals` (n_iter_max, may be NULL),
  * `*n_iter` the iterations run.  The least squares is a device Gram matrix
- * (FP64 sums) solved by Cholesky in FP64 with two refinement steps;
- * CUI_ERR_NUMERIC when that Gram matrix is not positive definite.  Allocates
+ * (FP64 sums) solved by a diagonally pivoted Cholesky in FP64 with two
+ * refinement steps; columns that are dependent to the Gram matrix's accuracy
+ * get coefficient 0, as the basic solution of the reference's pivoted-QR
+ * A \ y (cosamp.m:244) does for a rank-deficient A.  Allocates
  * device scratch of about (3s + 2) * N_obs + 2 * N_points values per call and
  * synchronises `stream` a few times per iteration. */
 cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* y, int32_t sparsity, int32_t n_iter_max,
