@@ -153,6 +153,10 @@ def roofline_of(args, info, kt, B, clk):
     hbm = {"compulsory_bytes": compulsory, "achieved_gbs": compulsory / t_launch / 1e9,
            "peak_gbs": pk["hbm_gbs"], "frac": compulsory / t_launch / 1e9 / pk["hbm_gbs"],
            "traffic_over_compulsory": (traffic / compulsory) if traffic else None}
+    # the reference writes Phi (8 B per complex entry) and reads it back through cublasCgemm: the
+    # rate at which this launch covers those bytes, against the HBM peak (the plain-FP32 criterion)
+    hbm["phi_equivalent_gbs"] = 8.0 * macs / t_launch / 1e9
+    hbm["phi_equivalent_frac"] = hbm["phi_equivalent_gbs"] / pk["hbm_gbs"]
     sm_mhz = clk.get("sm_mhz") or pk["sm_max_mhz"]
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     launch_ms = {"forward": kt["ms_forward"] / max(1, kt["n_forward"]),

@@ -67,12 +67,6 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
 
-__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
-    uint32_t v;
-    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
-    return v;
-}
-
 // wait by every lane of a producer warp; the result is made warp-uniform so that
 // the warp-wide tcgen05.ld that follows is always executed by all 32 lanes
 __device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
@@ -828,6 +822,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             tc::bar_arrive(ACCE + 8 * accs);
             return true;
         };
+        static_assert(C::LAG >= 1 && C::LAG <= C::NP, "the shared-role epilogue trails by LAG <= NP units");
         if constexpr (C::SPLIT) {
             if (h == 0) {
                 for (int it = 0; it < U && ok; ++it) ok = spread(it, 0, kProd / 2);
