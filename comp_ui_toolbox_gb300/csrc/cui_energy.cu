@@ -5,12 +5,15 @@
 //
 // Per observation row (slot s, mix m, local frequency fl) and grid point p:
 //   Phi[row, p] = p_in[s, p] * sum_{a in act(m)} pref[m][fl, a] * h(f_s; o(p, act_a), z_p)
-// and E[p] = sum_rows |Phi[row, p]|^2.  A block takes one grid line (y, z) and
-// a chunk of slots; per slot it stages the table rows of the frequency that the
-// line's elements reach (E_y rows of N_ox entries) and the line's incident
-// field in shared memory, then every thread accumulates the energies of its
-// points over the slot's rows.  Partial sums per slot chunk are reduced in a
-// fixed order (deterministic).
+// and E[p] = sum_rows |Phi[row, p]|^2 = sum_s |p_in[s, p]|^2 Q_s[p] with
+// Q_s[p] = sum_{rows of s} |sum_a pref h|^2.  Slots of one frequency whose rows
+// carry identical mixes share Q (the plan's energy groups: waves with a common
+// receive mixing), so Q is formed once per group.  A block takes one grid line
+// (y, z) and a chunk of groups; per group it stages the table rows of the
+// frequency that the line's elements reach (E_y rows of N_ox entries) in shared
+// memory, every thread forms Q for its points over the representative slot's
+// rows and adds |p_in|^2 Q for each slot of the group.  Partial sums per group
+// chunk are reduced in a fixed order (deterministic).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,6 +30,8 @@ struct EnergyArgs {
     const float2* table;    // [F][Nz][Noy][Nox]
     const float2* p_in;     // [S][P]
     const int* slot_f;
+    const int* egroup_ptr;
+    const int* egroup_slots;
     const int* slot_row_ptr;
     const int* slot_rows;
     const int* row_mix;
@@ -37,33 +42,36 @@ struct EnergyArgs {
     const int64_t* mix_pref_off;
     const int* act;
     const float2* pref;
-    int Nx, Ny, Nz, Ex, Ey, ppx, ppy, Nox, Noy, S, slots_per_chunk;
+    int Nx, Ny, Nz, Ex, Ey, ppx, ppy, Nox, Noy, n_groups, groups_per_chunk;
     int64_t P;
     float* part;            // [chunks][P]
 };
 
 __global__ void __launch_bounds__(kEnergyThreads) energy_kernel(const EnergyArgs a) {
     extern __shared__ float2 sm_e[];
-    float2* sT = sm_e;                             // [Ey][Nox]
-    float2* sP = sT + static_cast<size_t>(a.Ey) * a.Nox;  // [Nx]
+    float2* sT = sm_e;  // [Ey][Nox]
     const int line = blockIdx.x, chunk = blockIdx.y;
     const int iy = line % a.Ny, z = line / a.Ny;
     const int64_t pt0 = static_cast<int64_t>(line) * a.Nx;
-    const int s_lo = chunk * a.slots_per_chunk, s_hi = min(s_lo + a.slots_per_chunk, a.S);
+    const int g_lo = chunk * a.groups_per_chunk, g_hi = min(g_lo + a.groups_per_chunk, a.n_groups);
     float E[kEnergyMaxX];
 #pragma unroll
     for (int k = 0; k < kEnergyMaxX; ++k) E[k] = 0.f;
-    for (int s = s_lo; s < s_hi; ++s) {
-        const int f = a.slot_f[s];
+    for (int g = g_lo; g < g_hi; ++g) {
+        const int gb = a.egroup_ptr[g], ge = a.egroup_ptr[g + 1];
+        const int rep = a.egroup_slots[gb];
+        const int f = a.slot_f[rep];
         __syncthreads();
         for (int idx = threadIdx.x; idx < a.Ey * a.Nox; idx += blockDim.x) {
             const int ey = idx / a.Nox, ox = idx - ey * a.Nox;
             const int oy = iy - ey * a.ppy + (a.Ey - 1) * a.ppy;
             sT[idx] = a.table[((static_cast<int64_t>(f) * a.Nz + z) * a.Noy + oy) * a.Nox + ox];
         }
-        for (int x = threadIdx.x; x < a.Nx; x += blockDim.x) sP[x] = a.p_in[static_cast<int64_t>(s) * a.P + pt0 + x];
         __syncthreads();
-        for (int rr = a.slot_row_ptr[s]; rr < a.slot_row_ptr[s + 1]; ++rr) {
+        float Q[kEnergyMaxX];
+#pragma unroll
+        for (int k = 0; k < kEnergyMaxX; ++k) Q[k] = 0.f;
+        for (int rr = a.slot_row_ptr[rep]; rr < a.slot_row_ptr[rep + 1]; ++rr) {
             const int row = a.slot_rows[rr];
             const int m = a.row_mix[row], fl = a.row_fl[row];
             const int nact = a.mix_nact[m], nf = a.mix_nf[m];
@@ -74,7 +82,7 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_kernel(const EnergyArgs
             for (int k = 0; k < kEnergyMaxX; ++k) acc[k] = make_float2(0.f, 0.f);
             for (int ia = 0; ia < nact; ++ia) {
                 const int e = __ldg(act + ia);
-                const int ey = e / a.Ex, ex = e - ey * a.Ex;
+                const int ey = a.Ey == 1 ? 0 : e / a.Ex, ex = e - ey * a.Ex;
                 const float2 w = __ldg(pref + static_cast<int64_t>(ia) * nf);
                 const float2* trow = sT + ey * a.Nox + (a.Ex - 1 - ex) * a.ppx;
 #pragma unroll
@@ -88,11 +96,16 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_kernel(const EnergyArgs
                 }
             }
 #pragma unroll
+            for (int k = 0; k < kEnergyMaxX; ++k) Q[k] = fmaf(acc[k].x, acc[k].x, fmaf(acc[k].y, acc[k].y, Q[k]));
+        }
+        for (int i = gb; i < ge; ++i) {  // every slot of the group: |p_in|^2 Q
+            const float2* pin = a.p_in + static_cast<int64_t>(a.egroup_slots[i]) * a.P + pt0;
+#pragma unroll
             for (int k = 0; k < kEnergyMaxX; ++k) {
                 const int x = threadIdx.x + k * kEnergyThreads;
                 if (x < a.Nx) {
-                    const float2 pv = sP[x];
-                    E[k] = fmaf((pv.x * pv.x + pv.y * pv.y), (acc[k].x * acc[k].x + acc[k].y * acc[k].y), E[k]);
+                    const float2 pv = __ldg(pin + x);
+                    E[k] = fmaf(pv.x * pv.x + pv.y * pv.y, Q[k], E[k]);
                 }
             }
         }
@@ -127,17 +140,19 @@ extern "C" cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, voi
     const int lines = p.Ny * p.Nz;
     const int64_t cap = static_cast<int64_t>(p.ws_part_bytes / (sizeof(float) * static_cast<size_t>(p.P)));
     const int64_t want = (8 * 152 + lines - 1) / lines;
-    const int chunks0 = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({want, static_cast<int64_t>(p.S), cap})));
-    const int spc = (p.S + chunks0 - 1) / chunks0;
-    const int chunks = (p.S + spc - 1) / spc;
+    const int ng = p.n_egroups;
+    const int chunks0 = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({want, static_cast<int64_t>(ng), cap})));
+    const int gpc = std::max(1, (ng + chunks0 - 1) / chunks0);
+    const int chunks = std::max(1, (ng + gpc - 1) / gpc);
     EnergyArgs a;
     a.table = p.table; a.p_in = p.p_in; a.slot_f = p.slot_f; a.slot_row_ptr = p.slot_row_ptr; a.slot_rows = p.slot_rows;
+    a.egroup_ptr = p.egroup_ptr; a.egroup_slots = p.egroup_slots;
     a.row_mix = p.row_mix; a.row_fl = p.row_fl; a.mix_nact = p.mix_nact; a.mix_nf = p.mix_nf;
     a.mix_act_off = p.mix_act_off; a.mix_pref_off = p.mix_pref_off; a.act = p.act; a.pref = p.pref;
     a.Nx = p.Nx; a.Ny = p.Ny; a.Nz = p.Nz; a.Ex = p.Ex; a.Ey = p.Ey; a.ppx = p.ppx; a.ppy = p.ppy;
-    a.Nox = p.Nox; a.Noy = p.Noy; a.S = p.S; a.slots_per_chunk = spc; a.P = p.P;
+    a.Nox = p.Nox; a.Noy = p.Noy; a.n_groups = ng; a.groups_per_chunk = gpc; a.P = p.P;
     a.part = reinterpret_cast<float*>(p.ws_part);
-    const size_t smem = sizeof(float2) * (static_cast<size_t>(p.Ey) * p.Nox + p.Nx);
+    const size_t smem = sizeof(float2) * static_cast<size_t>(p.Ey) * p.Nox;
     if ((e = cudaFuncSetAttribute(energy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) !=
         cudaSuccess)
         return check_cuda(e, "energy_rx shared memory");

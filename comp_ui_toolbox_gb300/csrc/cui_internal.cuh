@@ -77,6 +77,11 @@ struct Plan {
     int* pos = nullptr;             // [n_mix][E] position of element in mix or -1
     int* slot_row_ptr = nullptr;    // [S+1] CSR of observations per slot
     int* slot_rows = nullptr;       // [n_obs]
+    // slots of one frequency whose rows carry identical mixes (active elements and prefactors),
+    // as CSR over groups: they differ only in their incident fields (received energies)
+    int n_egroups = 0;
+    int* egroup_ptr = nullptr;      // [n_egroups + 1]
+    int* egroup_slots = nullptr;    // [S], the first slot of a group is its representative
 
     // workspace (sized for max_objects at creation; shared by all applies)
     float2* ws_part = nullptr;      // forward / adjoint partial sums

@@ -341,6 +341,53 @@ cui_status select_device_and_shapes(Plan& p, int device) {
     return CUI_OK;
 }
 
+// Slots of one frequency whose observation rows carry identical mixes -- the same active
+// elements and bitwise the same prefactors, row by row -- have the same per-row sums
+// sum_a pref h in every column of Phi; only their incident fields differ.  The groups let the
+// received energies form those sums once per group (waves that share a receive mixing).
+static void energy_groups(const Plan& p, const HostMeta& h, std::vector<int>& gptr, std::vector<int>& gslots) {
+    auto same_rows = [&](int s1, int s2) {
+        const int b1 = h.slot_row_ptr[s1], n1 = h.slot_row_ptr[s1 + 1] - b1;
+        const int b2 = h.slot_row_ptr[s2], n2 = h.slot_row_ptr[s2 + 1] - b2;
+        if (n1 != n2) return false;
+        for (int k = 0; k < n1; ++k) {
+            const int r1 = h.slot_rows[b1 + k], r2 = h.slot_rows[b2 + k];
+            const int m1 = h.row_mix[r1], m2 = h.row_mix[r2];
+            const int na = h.mix_nact[m1];
+            if (na != h.mix_nact[m2]) return false;
+            if (m1 == m2 && h.row_fl[r1] == h.row_fl[r2]) continue;
+            if (std::memcmp(&h.act[h.mix_act_off[m1]], &h.act[h.mix_act_off[m2]], sizeof(int) * na) != 0) return false;
+            const int64_t o1 = h.mix_pref_off[m1] + h.row_fl[r1], o2 = h.mix_pref_off[m2] + h.row_fl[r2];
+            const int nf1 = h.mix_nf[m1], nf2 = h.mix_nf[m2];
+            for (int ia = 0; ia < na; ++ia)
+                if (std::memcmp(&h.pref[o1 + static_cast<int64_t>(ia) * nf1], &h.pref[o2 + static_cast<int64_t>(ia) * nf2],
+                                sizeof(float2)) != 0)
+                    return false;
+        }
+        return true;
+    };
+    gptr.assign(1, 0);
+    gslots.clear();
+    for (int f = 0; f < p.F; ++f) {
+        std::vector<std::vector<int>> groups;  // of this frequency, in first-seen order
+        for (int i = p.h_f_slot_ptr[f]; i < p.h_f_slot_ptr[f + 1]; ++i) {
+            const int s = p.h_f_slot_list[i];
+            bool placed = false;
+            for (auto& g : groups)
+                if (same_rows(g[0], s)) {
+                    g.push_back(s);
+                    placed = true;
+                    break;
+                }
+            if (!placed) groups.push_back({s});
+        }
+        for (const auto& g : groups) {
+            gslots.insert(gslots.end(), g.begin(), g.end());
+            gptr.push_back(static_cast<int>(gslots.size()));
+        }
+    }
+}
+
 cui_status upload_metadata_and_workspace(Plan& p) {
     HostMeta& h = p.h_meta;
     CUI_TRY(upload(p, &p.f_slot_ptr, p.h_f_slot_ptr));
@@ -358,6 +405,13 @@ cui_status upload_metadata_and_workspace(Plan& p) {
     CUI_TRY(upload(p, &p.pos, h.pos));
     CUI_TRY(upload(p, &p.slot_row_ptr, h.slot_row_ptr));
     CUI_TRY(upload(p, &p.slot_rows, h.slot_rows));
+    {
+        std::vector<int> gptr, gslots;
+        energy_groups(p, h, gptr, gslots);
+        p.n_egroups = static_cast<int>(gptr.size()) - 1;
+        CUI_TRY(upload(p, &p.egroup_ptr, gptr));
+        CUI_TRY(upload(p, &p.egroup_slots, gslots));
+    }
     p.h_meta = HostMeta();
 
     const int B = p.max_objects;
