@@ -247,13 +247,15 @@ class ClockSampler:
 
 
 # bounded CPU sample per workload (waves, frequencies, receive mixes): about 10-30 s of host work
-CPU_SAMPLE = {"2d-plain": (1, 8, None), "2d-gradient": (1, 8, None), "2d-batched": (1, 1, 8), "3d": (1, 1, None)}
+# bounded CPU samples: (waves, frequencies, receive mixes or None = all, axial planes or None = all)
+CPU_SAMPLE = {"2d-plain": (1, 8, None, None), "2d-gradient": (1, 8, None, None), "2d-batched": (1, 1, 8, None),
+              "3d": (1, 1, None, 4)}
 
 
 def cpu_baseline(workload: str, n_objects: int):
     from oracle.cpu_baseline import time_sample
-    nw, nf, nm = CPU_SAMPLE[workload]
-    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm)
+    nw, nf, nm, npl = CPU_SAMPLE[workload]
+    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm, n_planes=npl)
     return {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
             "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
 
@@ -275,8 +277,8 @@ def run_reference(args):
     w = workload(args.workload)
     B = w.n_objects if args.workload == "2d-batched" else 1
     from oracle.cpu_baseline import time_sample
-    nw, nf, nm = CPU_SAMPLE[args.workload]
-    first = time_sample(ORACLE_NAME[args.workload], n_waves=nw, n_freq=nf, n_objects=B, n_mixes=nm,
+    nw, nf, nm, npl = CPU_SAMPLE[args.workload]
+    first = time_sample(ORACLE_NAME[args.workload], n_waves=nw, n_freq=nf, n_objects=B, n_mixes=nm, n_planes=npl,
                         repeats=max(1, min(3, args.warmup + args.steps)))
     t_full = first["seconds_full_apply"]
     value = first["applies_per_s"]

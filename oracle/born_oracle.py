@@ -288,19 +288,19 @@ def shift_lateral(setup: Setup):
     # 1-based subscripts of all grid points, column-major
     subs = np.stack(np.unravel_index(np.arange(setup.n_points), tuple(N), order="F"), axis=1) + 1
     esubs = np.stack(np.unravel_index(np.arange(setup.n_elements), tuple(Eax), order="F"), axis=1) + 1
-    shifted = np.repeat(subs[:, None, :], setup.n_elements, axis=1).astype(np.int64)
-    for d in range(nl):
-        shifted[:, :, d] -= (esubs[None, :, d] - 1) * ppp[d]
-        offset = N[d] - (Eax[d] - 1) * ppp[d] + 1
-        ind = shifted[:, :, d] <= 0
-        shifted[:, :, d] = np.where(ind, offset - shifted[:, :, d], shifted[:, :, d])
-    valid = bool(np.all((shifted >= 1) & (shifted <= N[None, None, :])))
-    clipped = np.clip(shifted, 1, N[None, None, :])
+    # one grid axis at a time, broadcast over (points, elements)
     lin = np.zeros((setup.n_points, setup.n_elements), dtype=np.int64)
+    valid = True
     stride = 1
     for d in range(setup.n_dims):
-        lin += (clipped[:, :, d] - 1) * stride
-        stride *= N[d]
+        sd = subs[:, d].astype(np.int64)[:, None]
+        if d < nl:
+            sd = sd - (esubs[None, :, d].astype(np.int64) - 1) * ppp[d]
+            offset = N[d] - (Eax[d] - 1) * ppp[d] + 1
+            sd = np.where(sd <= 0, offset - sd, sd)
+        valid = valid and bool(np.all((sd >= 1) & (sd <= N[d])))
+        lin += (np.clip(sd, 1, N[d]) - 1) * stride
+        stride *= int(N[d])
     return lin + 1, valid
 
 

@@ -27,20 +27,27 @@ import numpy as np
 _STATE = {}
 
 
-def _sample_config(name: str, n_waves: int, n_freq: int):
+def _sample_config(name: str, n_waves: int, n_freq: int, n_planes=None):
+    """The workload restricted to n_waves waves, n_freq frequencies and (optionally) the first
+    n_planes axial grid planes; every grid point costs the same work, so the planes scale
+    linearly."""
+    import dataclasses
     from oracle import configs
     cfg = configs.config(name)
     f_idx = np.linspace(0, len(cfg.f) - 1, n_freq).round().astype(int)
     cfg.f = cfg.f[f_idx]
     cfg.waves = cfg.waves[:n_waves]
+    if n_planes is not None:
+        axes = tuple(cfg.setup.n_points_axis)
+        cfg.setup = dataclasses.replace(cfg.setup, n_points_axis=axes[:-1] + (min(n_planes, axes[-1]),))
     return cfg
 
 
-def _init(name, n_waves, n_freq, seed, n_objects=1):
+def _init(name, n_waves, n_freq, seed, n_objects=1, n_planes=None):
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     from oracle import configs
-    cfg = _sample_config(name, n_waves, n_freq)
+    cfg = _sample_config(name, n_waves, n_freq, n_planes)
     b = configs.build(cfg)
     rng = np.random.default_rng(seed)
     P = cfg.setup.n_points
@@ -65,18 +72,22 @@ def _work(args):
 
 
 def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: int | None = None,
-                repeats: int = 1, seed: int = 0, n_objects: int = 1, n_mixes: int | None = None):
+                repeats: int = 1, seed: int = 0, n_objects: int = 1, n_mixes: int | None = None,
+                n_planes: int | None = None):
     """Seconds per forward+adjoint apply of the full workload, extrapolated from a sample.
 
     ``n_mixes`` keeps only the first receive mixes of every wave (work is linear
     in the mixes when every mix has the same active elements, as in the
-    benchmark workloads).  Returns a dict with the sample description, the
+    benchmark workloads); ``n_planes`` keeps only the first axial grid planes
+    (work is linear in the grid points).  Returns a dict with the sample description, the
     measured seconds and the extrapolated full-workload applies/s.
     """
     from oracle import configs
     full = configs.config(name)
     S_full = len(full.waves) * len(full.f)
     S_sample = n_waves * n_freq
+    P_full = full.setup.n_points
+    P_sample = _sample_config(name, n_waves, n_freq, n_planes).setup.n_points
     n_mix_full = full.setup.n_elements if full.mixing == "identity" else full.n_mixes
     n_mix = min(n_mix_full, n_mixes or n_mix_full)
     procs = processes or os.cpu_count() or 1
@@ -87,25 +98,28 @@ def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: 
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[var] = "1"
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed, n_objects)) as pool:
+    with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed, n_objects, n_planes)) as pool:
         pool.map(_work, [(0, 0)] * procs)  # wait until every worker holds its tables
         times = []
         for _ in range(repeats):
             # critical path of the parallel apply: the slowest worker's own compute time
             times.append(max(t for t, _ in pool.map(_work, chunks, chunksize=1)))
     t_sample = min(times)
-    t_full = t_sample * (S_full / S_sample) * (n_mix_full / n_mix)
+    t_full = t_sample * (S_full / S_sample) * (n_mix_full / n_mix) * (P_full / P_sample)
     return {
         "seconds_sample": t_sample,
         "seconds_full_apply": t_full,
         "applies_per_s": n_objects / t_full,  # object-applies: all columns go through one BLAS call per element
         "cores": procs,
         "sample": f"{n_waves} of {len(full.waves)} waves x {n_freq} of {len(full.f)} frequencies x {n_objects} "
-                  f"gamma columns, full "
-                  f"{'x'.join(map(str, full.setup.n_points_axis))} grid, all {full.setup.n_elements} elements; "
+                  f"gamma columns, "
+                  + (f"full {'x'.join(map(str, full.setup.n_points_axis))} grid"
+                     if P_sample == P_full else f"{P_sample} of {P_full} grid points (the first {n_planes} axial planes)")
+                  + f", all {full.setup.n_elements} elements; "
                   f"one forward + one adjoint (FP64 numpy/scipy restatement of forward_quick_cpu/adjoint_quick_cpu), "
                   f"{n_mix} of {n_mix_full} receive mixes split over {procs} spawn processes; full-workload rate = "
-                  f"sample rate x {S_sample}/{S_full} x {n_mix}/{n_mix_full}",
+                  f"sample rate x {S_sample}/{S_full} x {n_mix}/{n_mix_full}"
+                  + (f" x {P_sample}/{P_full}" if P_sample != P_full else ""),
     }
 
 
