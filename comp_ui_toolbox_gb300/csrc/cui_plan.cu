@@ -310,7 +310,10 @@ cui_status select_device_and_shapes(Plan& p, int device) {
     const int n_lines = p.Ny * p.Nz;
     const int64_t gsz = static_cast<int64_t>(p.S) * p.max_objects * p.E * sizeof(float2);
     const int n_eyb = (p.Ey + fwd_rows_per_block(p.Ey) - 1) / fwd_rows_per_block(p.Ey);  // blocks per line group
-    int groups = std::max(1, std::min(n_lines, (2048 + p.F * n_eyb - 1) / (p.F * n_eyb)));
+    // about 2048 forward blocks, and at most 256 grid lines per group: each group is one FP32
+    // accumulation chain per element, and the 3D array's 16384 lines in 4 groups left chains of
+    // ~90k terms (partial sums are then added in a fixed order)
+    int groups = std::max(1, std::min(n_lines, std::max((2048 + p.F * n_eyb - 1) / (p.F * n_eyb), (n_lines + 255) / 256)));
     groups = static_cast<int>(std::max<int64_t>(
         1, std::min<int64_t>(groups, std::max<int64_t>(1, static_cast<int64_t>(kPartBudget) / std::max<int64_t>(gsz, 1)))));
     p.fwd_lines_per_group = (n_lines + groups - 1) / groups;
