@@ -3,13 +3,22 @@
 // combined_quick_gpu converts its FP64 input to FP32 on the host, uploads
 // it, runs the operator and converts the FP32 result back to FP64
 // (+scattering/combined_quick_gpu.cu:700-780, :940-1006).  These entry points
-// do the same around the device applies, with pinned staging buffers that
-// the plan allocates on first use and keeps.  The FP64 <-> FP32 conversions
-// run on all host cores, and the upload of gamma overlaps the conversion of
-// the measured data.
+// do the same around the device applies, in one of two ways:
+//   * where the GPU reads pageable host memory through the host's page tables
+//     (ATS over NVLink-C2C on Grace systems: cudaDevAttrPageableMemoryAccess and
+//     cudaDevAttrPageableMemoryAccessUsesHostPageTables), a kernel reads the
+//     caller's FP64 arrays and writes FP32 device columns, and another writes
+//     the FP64 result straight into the caller's array: no host pass and no
+//     staging copy;
+//   * otherwise through pinned staging buffers that the plan allocates on first
+//     use and keeps; the conversions run on all host cores, and the upload of
+//     gamma overlaps the conversion of the measured data.
+// The environment variable CUI_BORN_HOST_STAGING=1, read when a plan first
+// uses a host entry point, selects the staging path.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -20,15 +29,56 @@
 namespace cui {
 namespace {
 
-cui_status ensure_stage(Plan& p) {
-    if (p.h_stage_in) return CUI_OK;
+bool host_direct(Plan& p) {
+    if (p.host_direct < 0) {
+        int pageable = 0, host_tables = 0;
+        const char* env = std::getenv("CUI_BORN_HOST_STAGING");
+        const bool staging = env && env[0] == '1';
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p.device) != cudaSuccess) pageable = 0;
+        if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, p.device) !=
+            cudaSuccess)
+            host_tables = 0;
+        p.host_direct = (!staging && pageable && host_tables) ? 1 : 0;
+    }
+    return p.host_direct == 1;
+}
+
+// FP64 host column-major (leading dimension ld) -> packed FP32 device columns; grid (row blocks, B)
+__global__ void host_in_kernel(const cui_complex64* __restrict__ src, int64_t ld, int64_t rows, float2* __restrict__ dst) {
+    const int b = blockIdx.y;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const cui_complex64 c = src[b * ld + i];
+        dst[b * rows + i] = make_float2(static_cast<float>(c.re), static_cast<float>(c.im));
+    }
+}
+
+// packed FP32 device columns -> FP64 host column-major
+__global__ void host_out_kernel(const float2* __restrict__ src, int64_t rows, cui_complex64* __restrict__ dst, int64_t ld) {
+    const int b = blockIdx.y;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float2 v = src[b * rows + i];
+        cui_complex64 c;
+        c.re = v.x;
+        c.im = v.y;
+        dst[b * ld + i] = c;
+    }
+}
+
+__global__ void host_loss_kernel(const float* __restrict__ src, int B, double* __restrict__ dst) {
+    for (int b = threadIdx.x; b < B; b += blockDim.x) dst[b] = src[b];
+}
+
+dim3 host_grid(int64_t rows, int B) {
+    return dim3(static_cast<unsigned>(std::min<int64_t>((rows + 255) / 256, 4 * 152)), static_cast<unsigned>(B));
+}
+
+// device staging columns (both paths) and, for the staging path, the pinned host buffers
+cui_status ensure_device_stage(Plan& p) {
+    if (p.d_stage_in) return CUI_OK;
     const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
-    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_in), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
-    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_out), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
-    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_aux), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    cudaError_t e;
     void* v = nullptr;
     for (float2** d : {&p.d_stage_in, &p.d_stage_out, &p.d_stage_aux}) {
         if ((e = cudaMalloc(&v, n * sizeof(float2))) != cudaSuccess) return check_cuda(e, "cudaMalloc");
@@ -38,6 +88,19 @@ cui_status ensure_stage(Plan& p) {
     if ((e = cudaMalloc(&v, sizeof(float) * p.max_objects)) != cudaSuccess) return check_cuda(e, "cudaMalloc");
     p.allocations.push_back(v);
     p.d_stage_loss = static_cast<float*>(v);
+    return CUI_OK;
+}
+
+cui_status ensure_stage(Plan& p) {
+    cui_status s = ensure_device_stage(p);
+    if (s != CUI_OK || p.h_stage_in) return s;
+    const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_in), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_out), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_aux), n * sizeof(float2), cudaHostAllocDefault);
+    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
     p.h_stage_elems = n;
     return CUI_OK;
 }
@@ -99,6 +162,20 @@ cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_c
                                               "(combined_quick_gpu:NoValidDoubleMatrix)");
     cudaError_t e = cudaSetDevice(p.device);
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    if (host_direct(p)) {
+        cui_status s = ensure_device_stage(p);
+        if (s != CUI_OK) return s;
+        host_in_kernel<<<host_grid(rows_in, n_objects), 256>>>(input, ld_in, rows_in, p.d_stage_in);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
+        s = (mode == 1) ? forward_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0)
+                        : adjoint_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0);
+        if (s != CUI_OK) return s;
+        host_out_kernel<<<host_grid(rows_out, n_objects), 256>>>(p.d_stage_out, rows_out, output, ld_out);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host output");
+        return check_cuda(cudaStreamSynchronize(0), "synchronize");
+    }
     cui_status s = ensure_stage(p);
     if (s != CUI_OK) return s;
     pack(input, ld_in, rows_in, n_objects, p.h_stage_in);
@@ -127,6 +204,24 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
         return set_error(CUI_ERR_INVALID_ARG, "invalid arguments to cui_born_vjp_host");
     cudaError_t e = cudaSetDevice(p.device);
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    if (host_direct(p)) {
+        cui_status s = ensure_device_stage(p);
+        if (s != CUI_OK) return s;
+        host_in_kernel<<<host_grid(p.P, n_objects), 256>>>(gamma, ld_gamma, p.P, p.d_stage_in);
+        host_in_kernel<<<host_grid(p.n_obs, n_objects), 256>>>(u_meas, ld_u, p.n_obs, p.d_stage_aux);
+        count_launch(2);
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
+        s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0);
+        if (s != CUI_OK) return s;
+        host_out_kernel<<<host_grid(p.P, n_objects), 256>>>(p.d_stage_out, p.P, grad, ld_grad);
+        count_launch();
+        if (loss) {
+            host_loss_kernel<<<1, 128>>>(p.d_stage_loss, n_objects, loss);
+            count_launch();
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host output");
+        return check_cuda(cudaStreamSynchronize(0), "synchronize");
+    }
     cui_status s = ensure_stage(p);
     if (s != CUI_OK) return s;
     // gamma and u_meas share the input staging buffer: gamma first, then u_meas

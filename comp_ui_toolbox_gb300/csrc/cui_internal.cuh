@@ -106,6 +106,7 @@ struct Plan {
     float2* h_stage_out = nullptr;
     float2* h_stage_aux = nullptr;   // second input staging buffer (measured data of the host VJP)
     size_t h_stage_elems = 0;
+    int host_direct = -1;            // host entry points: kernels read/write the caller's buffers (-1: not probed)
     float2* d_stage_in = nullptr;   // device copies for the host entry points
     float2* d_stage_out = nullptr;
     float2* d_stage_aux = nullptr;

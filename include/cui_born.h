@@ -295,7 +295,11 @@ cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* y, int32_t 
  * output = combined_quick_gpu(operator_born, mode, input): mode 1 forward
  * (input N_points x n_objects), mode 2 adjoint (input N_obs x n_objects).
  * Host buffers in MATLAB's interleaved complex double; FP64 <-> FP32
- * conversion and host <-> device copies happen inside, synchronously. */
+ * conversion and host <-> device copies happen inside, synchronously.  Where
+ * the GPU reads pageable host memory through the host's page tables (Grace
+ * systems: ATS over NVLink-C2C), kernels read the caller's arrays and write
+ * the result into them directly; elsewhere the data pass through pinned
+ * staging buffers the plan keeps (also selected by CUI_BORN_HOST_STAGING=1). */
 cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_complex64* input,
                                   int64_t ld_in, int32_t n_objects, cui_complex64* output, int64_t ld_out);
 

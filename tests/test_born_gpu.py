@@ -76,6 +76,33 @@ def test_batched_mixing_matches_oracle(name, B):
     assert op.device_status() == 0
 
 
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("staging", ["direct", "staging"])
+def test_host_vjp_matches_device_vjp(precision, staging, monkeypatch):
+    """cui_born_vjp_host on 20 objects, through both host paths (direct access to the caller's
+    arrays, or pinned staging), against the device VJP of the same objects: the same device
+    computation, so equal to rounding of the FP64 <-> FP32 conversions (relative 1e-6), and
+    within the operator's bound of the oracle."""
+    monkeypatch.setenv("CUI_BORN_HOST_STAGING", "1" if staging == "staging" else "0")
+    b = built("c2")
+    B = 20
+    op = make_operator(b, "lateral", max_objects=B)
+    op.set_precision(precision)
+    gamma = configs.make_gamma(b.cfg, n_objects=B, seed=31)
+    u_meas = rand_obs(b, B, 32)
+    grad_d, loss_d = op.vjp(dev(gamma), dev(u_meas))
+    grad_d = grad_d.cpu().numpy()
+    loss_d = loss_d.cpu().numpy()
+    grad_h, loss_h = op.vjp(gamma, u_meas)
+    r = forward_quick_cpu(b.op, gamma) - u_meas
+    g_ref = adjoint_quick_cpu(b.op, r)
+    for k in range(B):
+        assert rel_l2(grad_h[:, k], grad_d[:, k]) <= 1e-6
+        assert rel_l2(grad_h[:, k], g_ref[:, k]) <= TOL
+    np.testing.assert_allclose(loss_h, loss_d, rtol=1e-6)
+    assert op.device_status() == 0
+
+
 @pytest.mark.parametrize("name", ["c1", "c2", "ragged", "c3"])
 def test_reference_form_matches_lateral_form(name):
     """The reference's h_ref + indices_grid_FOV_shift give the same operator."""
@@ -91,8 +118,12 @@ def test_reference_form_matches_lateral_form(name):
 
 
 @pytest.mark.parametrize("name", ["c1", "ragged"])
-def test_host_path_matches_oracle(name):
-    """FP64 host buffers in, FP64 out: the MEX gateway's semantics."""
+@pytest.mark.parametrize("staging", ["direct", "staging"])
+def test_host_path_matches_oracle(name, staging, monkeypatch):
+    """FP64 host buffers in, FP64 out: the MEX gateway's semantics.  Both host paths: kernels that
+    read and write the caller's pageable arrays (where the GPU uses the host's page tables) and
+    the pinned staging buffers (CUI_BORN_HOST_STAGING=1)."""
+    monkeypatch.setenv("CUI_BORN_HOST_STAGING", "1" if staging == "staging" else "0")
     b = built(name)
     B = b.cfg.n_objects
     op = make_operator(b, "lateral", max_objects=B)
