@@ -347,7 +347,65 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
         const uint32_t lane_addr = static_cast<uint32_t>(qd * 32) << 16;
         bool ok = true;
         for (int q = 0; q < Q + C::LAG && ok; ++q) {
-            if (q < Q) {
+            if (q < Q && NT == 64) {
+                // 64-column tiles (4 objects x 16 slots): thread = (slot sl, 4-point group g4s), so each
+                // slot's incident-field segment is read once and multiplied by the 4 objects' gamma
+                const int rs = q % C::NR, s = q % C::NS;
+                const int kc = q % nKC;
+                const int sl = tid & 15, g4s = tid >> 4;
+                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag))) break;
+                const uint32_t raw = sRaw + rs * L.RS;
+                const bool xin = kc * kKC + 4 * g4s < a.Nx;
+                float4 pv[2], gv[4][2];
+                if (xin && sl < ns) {
+                    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                 : "=f"(pv[0].x), "=f"(pv[0].y), "=f"(pv[0].z), "=f"(pv[0].w)
+                                 : "r"(raw + sl * kRawRow + 32 * g4s) : "memory");
+                    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                 : "=f"(pv[1].x), "=f"(pv[1].y), "=f"(pv[1].z), "=f"(pv[1].w)
+                                 : "r"(raw + sl * kRawRow + 32 * g4s + 16) : "memory");
+                } else {
+                    pv[0] = pv[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int bl = 0; bl < 4; ++bl) {
+                    if (xin && bl < nb) {
+                        const uint32_t ga = raw + a.ms * kRawRow + bl * 512 + 32 * g4s;
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(gv[bl][0].x), "=f"(gv[bl][0].y), "=f"(gv[bl][0].z), "=f"(gv[bl][0].w)
+                                     : "r"(ga) : "memory");
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(gv[bl][1].x), "=f"(gv[bl][1].y), "=f"(gv[bl][1].z), "=f"(gv[bl][1].w)
+                                     : "r"(ga + 16) : "memory");
+                    } else {
+                        gv[bl][0] = gv[bl][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                }
+                tc::fence_async_smem();
+                tc::bar_arrive(RAWE + 8 * rs);
+                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag))) break;
+                const uint32_t bst = sB + s * C::STB;
+                const float pr[4] = {pv[0].x, pv[0].z, pv[1].x, pv[1].z};
+                const float pi[4] = {pv[0].y, pv[0].w, pv[1].y, pv[1].w};
+#pragma unroll
+                for (int bl = 0; bl < 4; ++bl) {
+                    const float gr[4] = {gv[bl][0].x, gv[bl][0].z, gv[bl][1].x, gv[bl][1].z};
+                    const float gi[4] = {gv[bl][0].y, gv[bl][0].w, gv[bl][1].y, gv[bl][1].w};
+                    uint32_t h1[4], l1[4];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const float qx = pr[t] * gr[t] - pi[t] * gi[t], qy = pr[t] * gi[t] + pi[t] * gr[t];
+                        split(qx, -qy, h1[t], l1[t]);
+                    }
+                    const int c = bl * 16 + sl;
+                    sts128(bst + b_off(c, g4s, C::SBO), h1[0], h1[1], h1[2], h1[3]);
+                    sts128(bst + b_off(NT + c, g4s, C::SBO), rot(h1[0]), rot(h1[1]), rot(h1[2]), rot(h1[3]));
+                    sts128(bst + b_off(2 * NT + c, g4s, C::SBO), l1[0], l1[1], l1[2], l1[3]);
+                    sts128(bst + b_off(3 * NT + c, g4s, C::SBO), rot(l1[0]), rot(l1[1]), rot(l1[2]), rot(l1[3]));
+                }
+                tc::fence_async_smem();
+                tc::bar_arrive(FULL + 8 * s);
+            } else if (q < Q) {
                 const int rs = q % C::NR, s = q % C::NS;
                 const int kc = q % nKC;
                 if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag))) break;
