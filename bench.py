@@ -51,8 +51,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--fp32-steps", type=int, default=3,
                     help="steps of the plain FP32 path timed after the main region (0: skip)")
-    ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default="bf16x3",
-                    help="adjoint contraction: FP32 CUDA cores or split-BF16 tcgen05 tensor cores")
+    ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default=None,
+                    help="contraction path: FP32 CUDA cores, split-BF16 tcgen05 tensor cores, or the per-plan "
+                         "autotuner (default: bf16x3 for 2d-batched, fp32 for 3d, auto otherwise)")
     ap.add_argument("--lasso-streams", type=int, default=4,
                     help="2d-lasso: concurrent streams the problems are spread over inside the graph")
     ap.add_argument("--lasso-problems", type=int, default=16,
@@ -323,9 +324,14 @@ def run_ours(args):
     snr = 10 ** (-30 / 20)
     u_meas = (u_clean + noise * (u_clean.abs().pow(2).mean().sqrt() / noise.abs().pow(2).mean().sqrt()) * snr).contiguous()
     gamma = torch.randn((P, B), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
+    autotune = None
+    if args.precision == "auto":  # the per-plan autotuner keeps the faster path; the bench then runs that
+        autotune = op.autotune(B)
+        args.precision = autotune["precision"]
     accuracy = None
     if args.precision != "fp32":
         # same plan, both precisions: relative L2 of the split-BF16 gradient against the FP32 one
+        op.set_precision("fp32")
         g32, _ = op.vjp(gamma, u_meas)
         op.set_precision(args.precision)
         gtc, _ = op.vjp(gamma, u_meas)
@@ -397,7 +403,8 @@ def run_ours(args):
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "clocks": clk,
             "plan": {"build_s": t_build, "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
                      "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs},
-            "loss": float(loss.sum().item()), "precision": args.precision, "accuracy": accuracy,
+            "loss": float(loss.sum().item()), "precision": args.precision, "autotune": autotune,
+            "accuracy": accuracy,
             "device_status": op.device_status()}
     if args.fp32_steps > 0 and args.precision != "fp32":
         # the plain FP32 path of the same plan on the same inputs: the split-BF16 speed-up
@@ -587,6 +594,8 @@ def run_lasso(args):
 
 def main():
     args = parse()
+    if args.precision is None:
+        args.precision = {"2d-batched": "bf16x3", "3d": "fp32"}.get(args.workload, "auto")
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "2d-lasso":
