@@ -54,6 +54,11 @@ def parse():
     ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default=None,
                     help="contraction path: FP32 CUDA cores, split-BF16 tcgen05 tensor cores, or the per-plan "
                          "autotuner (default: bf16x3 for 2d-batched, fp32 for 3d, auto otherwise)")
+    ap.add_argument("--table-storage", choices=["auto", "stored", "streamed", "generated"], default=None,
+                    help="lateral transfer-function table: stored once; regenerated every apply in chunks of "
+                         "frequencies (streamed, 3D); or generated inside the contraction kernels where they use "
+                         "it (3D); auto stores it unless it does not fit in device memory (default: streamed for "
+                         "3d, whose configuration recomputes the table; auto otherwise)")
     ap.add_argument("--lasso-streams", type=int, default=4,
                     help="2d-lasso: concurrent streams the problems are spread over inside the graph")
     ap.add_argument("--lasso-problems", type=int, default=16,
@@ -145,11 +150,16 @@ def roofline_of(args, info, kt, B, clk):
     dom = "forward" if kt["ms_forward"] >= kt["ms_adjoint"] else "adjoint"
     t_launch = kt["ms_" + dom] / max(1, kt["n_" + dom]) / 1e3
     P = info["n_points"]
-    compulsory = info["table_bytes"] + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
+    # table bytes one launch moves: a stored table is read once; a streamed one is written by the chunk
+    # generator and read back (the full table, chunk by chunk); a generated one never leaves the SMs
+    table = {"stored": info["table_bytes"], "streamed": 2 * args.full_table_bytes, "generated": 0}[args.table_used]
+    compulsory = table + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
     tc = args.precision != "fp32"
-    # every 2D benchmark workload (4 grid points per pitch, lines a multiple of 8) runs the line-unit kernels
+    # every 2D benchmark workload (4 grid points per pitch, lines a multiple of 8) runs the line-unit kernels;
+    # 3D setups run the FP32 kernels under register ceilings (dense3) or with the generator inside (gen)
+    fp32_kind = "dense" if args.n_dims == 2 else ("gen" if args.table_used == "generated" else "dense3")
     kernel = {("forward", True): "fwd_tc2_kernel", ("adjoint", True): "adj_tc2_kernel",
-              ("forward", False): "fwd_dense_kernel", ("adjoint", False): "adj_dense_kernel"}[(dom, tc)]
+              ("forward", False): f"fwd_{fp32_kind}_kernel", ("adjoint", False): f"adj_{fp32_kind}_kernel"}[(dom, tc)]
     traffic = launch_traffic(args.workload, kernel, args.n_freq_used)
     hbm = {"compulsory_bytes": compulsory, "achieved_gbs": compulsory / t_launch / 1e9,
            "peak_gbs": pk["hbm_gbs"], "frac": compulsory / t_launch / 1e9 / pk["hbm_gbs"],
@@ -261,6 +271,24 @@ def cpu_baseline(workload: str, n_objects: int):
             "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
 
 
+TABLE_STORAGE = {
+    "stored": "stored: built on the device once per plan, read every apply",
+    "streamed": "streamed: regenerated on the device every apply, one chunk of frequencies at a time into a "
+                "chunk buffer, then read by the contraction kernels (never stored whole)",
+    "generated": "generated: computed inside the contraction kernels where each entry is staged (never stored)",
+}
+
+
+def full_table_bytes(w) -> int:
+    """Bytes of the stored lateral table [F][Nz][Noy][Nox] (FP32 complex) of a workload."""
+    nl = len(w.n_points_axis) - 1
+    n = len(w.f) * w.n_points_axis[-1]
+    for a in range(nl):
+        ppp = int(round(w.pitch_axis[a] / w.delta_axis[a]))
+        n *= w.n_points_axis[a] + (w.n_elements_axis[a] - 1) * ppp
+    return 8 * n
+
+
 def workload_config(w, B):
     return {"workload": f"{w.name}: {'x'.join(map(str, w.n_points_axis))} FOV, {len(w.f)} frequencies, "
                         f"{w.n_elements} elements, {len(w.waves)} waves, {w.absorption['kind']} medium; "
@@ -311,9 +339,12 @@ def run_ours(args):
     args.n_freq_used = len(w.f)
     B = w.n_objects if args.workload == "2d-batched" else 1
     t0 = time.perf_counter()
-    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=B)
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=B, table_storage=args.table_storage)
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
+    args.table_used = op.table_storage
+    args.n_dims = len(w.n_points_axis)
+    args.full_table_bytes = full_table_bytes(w)
     P, N = op.n_points, op.n_observations
 
     # data: u = Phi gamma_true + 30 dB noise; the gradient is taken at a seeded Gaussian gamma
@@ -399,9 +430,10 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16x3 (split-BF16 operands, f32 accumulate)",
-            "data": "synthetic (seeded)", "config": workload_config(w, B),
+            "data": "synthetic (seeded)", "config": dict(workload_config(w, B), table_storage=TABLE_STORAGE[args.table_used]),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "clocks": clk,
-            "plan": {"build_s": t_build, "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
+            "plan": {"build_s": t_build, "table_storage": op.table_storage,
+                     "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
                      "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs},
             "loss": float(loss.sum().item()), "precision": args.precision, "autotune": autotune,
             "accuracy": accuracy,
@@ -596,6 +628,8 @@ def main():
     args = parse()
     if args.precision is None:
         args.precision = {"2d-batched": "bf16x3", "3d": "fp32"}.get(args.workload, "auto")
+    if args.table_storage is None:
+        args.table_storage = {"3d": "streamed"}.get(args.workload, "auto")
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "2d-lasso":

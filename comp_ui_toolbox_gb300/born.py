@@ -101,6 +101,9 @@ class BornInfo(C.Structure):
 
 _lib = None
 
+# cui_table_storage
+_TABLE_STORAGE = {"auto": 0, "stored": 1, "generated": 2, "streamed": 3}
+
 # every symbol include/cui_born.h declares, with its ctypes signature
 _SIGNATURES = {
     "cui_born_plan_create": (C.c_int, [C.POINTER(BornDesc), C.c_int32, C.POINTER(C.c_void_p)]),
@@ -108,6 +111,9 @@ _SIGNATURES = {
     "cui_born_plan_create_setup_cached": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.c_char_p,
                                                     C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]),
     "cui_born_setup_hash": (C.c_int, [C.POINTER(SetupDesc), C.c_char_p]),
+    "cui_born_plan_create_setup_ex": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.c_int32, C.c_char_p,
+                                                C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]),
+    "cui_born_plan_table_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "cui_born_plan_destroy": (C.c_int, [C.c_void_p]),
     "cui_born_plan_info": (C.c_int, [C.c_void_p, C.POINTER(BornInfo)]),
     "cui_born_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -268,7 +274,7 @@ class OperatorBorn:
 
     @classmethod
     def from_setup(cls, *, device: int = 0, max_objects: int = 1, cache_dir: Optional[str] = None,
-                   **setup) -> "OperatorBorn":
+                   table_storage: str = "auto", **setup) -> "OperatorBorn":
         """Plan whose tables the GPU computes from the discretised setup (``setup_desc`` lists
         the keyword arguments).
 
@@ -277,6 +283,12 @@ class OperatorBorn:
         incident fields are loaded from ``cache_dir/cui_born_<setup hash>.tables`` when that
         file exists, else computed and stored there.  ``loaded_from_cache`` is then 1 (loaded),
         0 (computed and stored) or -1 (computed; storing failed).
+
+        ``table_storage`` (``cui_born_plan_create_setup_ex``): ``"stored"`` builds the lateral
+        table once; ``"streamed"`` (3D setups) regenerates it every apply one chunk of
+        frequencies at a time into a chunk buffer; ``"generated"`` (3D) never stores any of it,
+        the kernels compute each entry where they use it; ``"auto"`` stores it unless it does
+        not fit in device memory.  ``self.table_storage`` says which the plan uses.
         """
         self = cls.__new__(cls)
         lib = load_library()
@@ -284,15 +296,21 @@ class OperatorBorn:
         self._plan = C.c_void_p()
         d, keep = setup_desc(device=device, **setup)
         self.loaded_from_cache = None
-        if cache_dir is None:
+        storage = _TABLE_STORAGE[table_storage]
+        if cache_dir is None and storage == 0:
             _check(lib.cui_born_plan_create_setup(C.byref(d), int(max_objects), C.byref(self._plan)))
         else:
             loaded = C.c_int32(0)
-            _check(lib.cui_born_plan_create_setup_cached(C.byref(d), int(max_objects), str(cache_dir).encode(),
-                                                         C.byref(self._plan), C.byref(loaded)))
-            self.loaded_from_cache = loaded.value
+            _check(lib.cui_born_plan_create_setup_ex(C.byref(d), int(max_objects), storage,
+                                                     None if cache_dir is None else str(cache_dir).encode(),
+                                                     C.byref(self._plan), C.byref(loaded)))
+            if cache_dir is not None:
+                self.loaded_from_cache = loaded.value
         del keep
         self._finish(max_objects, device)
+        mode = C.c_int32(0)
+        _check(lib.cui_born_plan_table_storage(self._plan, C.byref(mode)))
+        self.table_storage = {v: k for k, v in _TABLE_STORAGE.items()}[mode.value]
         return self
 
     def _finish(self, max_objects, device):
@@ -304,6 +322,7 @@ class OperatorBorn:
         self.n_observations = self.info["n_observations"]
         self.n_points = self.info["n_points"]
         self.device = int(device)
+        self.table_storage = "stored"
 
     # ------------------------------------------------------------------
     def close(self):

@@ -115,12 +115,12 @@ uint64_t key_hash(const std::vector<unsigned char>& key) {
     return h;
 }
 
-std::string cache_path(const char* dir, const std::vector<unsigned char>& key) {
+std::string cache_path(const char* dir, const std::vector<unsigned char>& key, bool incident_only) {
     char hex[17];
     std::snprintf(hex, sizeof hex, "%016llx", static_cast<unsigned long long>(key_hash(key)));
     std::string path(dir);
     if (!path.empty() && path.back() != '/') path += '/';
-    return path + "cui_born_" + hex + ".tables";
+    return path + "cui_born_" + hex + (incident_only ? ".incident" : ".tables");
 }
 
 cui_status cache_load(const std::string& path, const std::vector<unsigned char>& key, Plan& p, bool* hit) {
@@ -144,7 +144,7 @@ cui_status cache_load(const std::string& path, const std::vector<unsigned char>&
     cudaError_t e = cudaMallocHost(&stg.h, kChunk);
     if (e != cudaSuccess) return check_cuda(e, "cudaMallocHost (table cache)");
     void* dst[2] = {p.table, p.p_in};
-    const size_t want[2] = {p.table_bytes, p.incident_bytes};
+    const size_t want[2] = {p.table ? p.table_bytes : 0, p.incident_bytes};  // no table unless stored
     for (int a = 0; a < 2; ++a) {
         uint64_t n = 0;
         if (std::fread(&n, sizeof n, 1, fh.f) != 1 || n != want[a])
@@ -174,7 +174,7 @@ cui_status cache_store(const std::string& path, const std::vector<unsigned char>
         bool ok = std::fwrite(kMagic, 1, 8, fh.f) == 8 && std::fwrite(&klen, sizeof klen, 1, fh.f) == 1 &&
                   std::fwrite(key.data(), 1, key.size(), fh.f) == key.size();
         const void* src[2] = {p.table, p.p_in};
-        const size_t have[2] = {p.table_bytes, p.incident_bytes};
+        const size_t have[2] = {p.table ? p.table_bytes : 0, p.incident_bytes};
         for (int a = 0; a < 2 && ok; ++a) {
             const uint64_t n = have[a];
             ok = std::fwrite(&n, sizeof n, 1, fh.f) == 1;

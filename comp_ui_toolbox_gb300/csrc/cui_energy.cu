@@ -11,7 +11,7 @@
 // receive mixing), so Q is formed once per group.  A block takes one grid line
 // (y, z) and a chunk of groups; per group it stages the table rows of the
 // frequency that the line's elements reach (E_y rows of N_ox entries) in shared
-// memory, every thread forms Q for its points over the representative slot's
+// memory (read from the stored table or generated there), every thread forms Q for its points over the representative slot's
 // rows and adds |p_in|^2 Q for each slot of the group.  Partial sums per group
 // chunk are reduced in a fixed order (deterministic).
 #include <cuda_runtime.h>
@@ -27,7 +27,8 @@ constexpr int kEnergyThreads = 256;
 constexpr int kEnergyMaxX = 4;  // points per thread: lateral lines of up to 1024 points
 
 struct EnergyArgs {
-    const float2* table;    // [F][Nz][Noy][Nox]
+    const float2* table;    // [F][Nz][Noy][Nox], or null when generated (gen)
+    TableGen gen;
     const float2* p_in;     // [S][P]
     const int* slot_f;
     const int* egroup_ptr;
@@ -47,6 +48,7 @@ struct EnergyArgs {
     float* part;            // [chunks][P]
 };
 
+template <bool GEN>
 __global__ void __launch_bounds__(kEnergyThreads) energy_kernel(const EnergyArgs a) {
     extern __shared__ float2 sm_e[];
     float2* sT = sm_e;  // [Ey][Nox]
@@ -65,7 +67,10 @@ __global__ void __launch_bounds__(kEnergyThreads) energy_kernel(const EnergyArgs
         for (int idx = threadIdx.x; idx < a.Ey * a.Nox; idx += blockDim.x) {
             const int ey = idx / a.Nox, ox = idx - ey * a.Nox;
             const int oy = iy - ey * a.ppy + (a.Ey - 1) * a.ppy;
-            sT[idx] = a.table[((static_cast<int64_t>(f) * a.Nz + z) * a.Noy + oy) * a.Nox + ox];
+            if constexpr (GEN)
+                sT[idx] = gen_entry(a.gen, gen_row(a.gen, f, z, oy), ox);
+            else
+                sT[idx] = a.table[((static_cast<int64_t>(f) * a.Nz + z) * a.Noy + oy) * a.Nox + ox];
         }
         __syncthreads();
         float Q[kEnergyMaxX];
@@ -145,7 +150,7 @@ extern "C" cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, voi
     const int gpc = std::max(1, (ng + chunks0 - 1) / chunks0);
     const int chunks = std::max(1, (ng + gpc - 1) / gpc);
     EnergyArgs a;
-    a.table = p.table; a.p_in = p.p_in; a.slot_f = p.slot_f; a.slot_row_ptr = p.slot_row_ptr; a.slot_rows = p.slot_rows;
+    a.table = p.table; a.gen = p.gen; a.p_in = p.p_in; a.slot_f = p.slot_f; a.slot_row_ptr = p.slot_row_ptr; a.slot_rows = p.slot_rows;
     a.egroup_ptr = p.egroup_ptr; a.egroup_slots = p.egroup_slots;
     a.row_mix = p.row_mix; a.row_fl = p.row_fl; a.mix_nact = p.mix_nact; a.mix_nf = p.mix_nf;
     a.mix_act_off = p.mix_act_off; a.mix_pref_off = p.mix_pref_off; a.act = p.act; a.pref = p.pref;
@@ -153,11 +158,11 @@ extern "C" cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, voi
     a.Nox = p.Nox; a.Noy = p.Noy; a.n_groups = ng; a.groups_per_chunk = gpc; a.P = p.P;
     a.part = reinterpret_cast<float*>(p.ws_part);
     const size_t smem = sizeof(float2) * static_cast<size_t>(p.Ey) * p.Nox;
-    if ((e = cudaFuncSetAttribute(energy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) !=
-        cudaSuccess)
+    void (*kern)(const EnergyArgs) = p.table_mode != CUI_STORAGE_STORED ? energy_kernel<true> : energy_kernel<false>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) != cudaSuccess)
         return check_cuda(e, "energy_rx shared memory");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    energy_kernel<<<dim3(lines, chunks), kEnergyThreads, smem, st>>>(a);
+    kern<<<dim3(lines, chunks), kEnergyThreads, smem, st>>>(a);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "energy_rx");
     energy_reduce_kernel<<<static_cast<int>(std::min<int64_t>((p.P + 255) / 256, 152 * 32)), 256, 0, st>>>(

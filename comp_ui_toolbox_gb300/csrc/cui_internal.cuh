@@ -3,6 +3,7 @@
 // Device layout of a plan (all FP32 complex as float2):
 //   table   [F][Nz][Noy][Nox]  lateral-offset transfer-function table; row (f, z, oy)
 //                              is contiguous in ox.  No_d = N_d + (E_d-1)*ppp_d.
+//                              Not stored when generated (cui_gen.cuh).
 //   p_in    [S][P]             incident field of each slot (measurement, unique
 //                              frequency), points in column-major grid order.
 //   rows    [n_obs]            observation -> (slot, mix, local frequency).
@@ -20,6 +21,7 @@
 #include <vector>
 
 #include "../../include/cui_born.h"
+#include "cui_gen.cuh"
 
 namespace cui {
 
@@ -60,7 +62,11 @@ struct Plan {
     int max_slots_per_f = 0;
 
     // device tables
-    float2* table = nullptr;
+    float2* table = nullptr;        // null unless the table is stored
+    int table_mode = CUI_STORAGE_STORED;  // or CUI_STORAGE_GENERATED / CUI_STORAGE_STREAMED (3D setup form)
+    TableGen gen{};                 // generator parameters (device arrays) when not stored
+    float2* stream_buf = nullptr;   // streamed: table rows of stream_nf frequencies, [stream_nf][Nz][Noy][Nox]
+    int stream_nf = 0;              // frequencies per streamed chunk (= adj_fchunk)
     float2* p_in = nullptr;
     int* f_slot_ptr = nullptr;      // [F+1] CSR of slots per global frequency
     int* f_slot_list = nullptr;     // [S]
@@ -166,10 +172,11 @@ cui_status select_device_and_shapes(Plan& p, int device);
 cui_status upload_metadata_and_workspace(Plan& p);
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes);
 // table cache (cui_cache.cu): canonical key of the setup fields the device tables depend on,
-// its file path under `dir`, and loading / storing p.table and p.p_in
+// its file path under `dir` (the incident fields alone when the table is not stored), and
+// loading / storing p.table (when stored) and p.p_in
 cui_status setup_key(const cui_born_setup_desc* d, std::vector<unsigned char>& key);
 uint64_t key_hash(const std::vector<unsigned char>& key);
-std::string cache_path(const char* dir, const std::vector<unsigned char>& key);
+std::string cache_path(const char* dir, const std::vector<unsigned char>& key, bool incident_only);
 cui_status cache_load(const std::string& path, const std::vector<unsigned char>& key, Plan& p, bool* hit);
 cui_status cache_store(const std::string& path, const std::vector<unsigned char>& key, const Plan& p);
 

@@ -72,12 +72,36 @@ __device__ __forceinline__ void stage_band(float2* sA, const float2* __restrict_
     }
 }
 
+// Same bands with the entries of row (f, z, oy) computed in place (generated table, 3D setups).
+__device__ __forceinline__ void stage_band_gen(float2* sA, const TableGen& t, int f, int z, int oy, const LineGeom& g) {
+    const GenRow row = gen_row(t, f, z, oy);
+    const int n = g.ppx * g.Ni;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int r = idx / g.Ni;
+        const int i = idx - r * g.Ni - kPad;
+        const int o = r + g.ppx * i;
+        sA[idx] = (i >= 0 && o < g.Nox) ? gen_entry(t, row, o) : make_float2(0.f, 0.f);
+    }
+}
+
+// Table row (f, z, oy) into the bands at sA: read from the stored table or generated.
+template <bool GEN>
+__device__ __forceinline__ void stage_row(float2* sA, const float2* __restrict__ table, int tab_f0, const TableGen& t,
+                                          int f, int z, int oy, const LineGeom& g) {
+    if constexpr (GEN)
+        stage_band_gen(sA, t, f, z, oy, g);
+    else
+        stage_band(sA, table + ((static_cast<int64_t>(f - tab_f0) * g.Nz + z) * g.Noy + oy) * g.Nox, g);
+}
+
 // ---------------------------------------------------------------------------
 // dense forward: block = (line group x ey, frequency, object x column pass)
 // ---------------------------------------------------------------------------
 struct FwdArgs {
     LineGeom g;
-    const float2* __restrict__ table;
+    const float2* __restrict__ table;  // stored table (frequencies from tab_f0 on), or null when generated (gen)
+    TableGen gen;
+    int f_base, tab_f0;                // frequency of blockIdx.y = 0; first frequency the table holds
     const float2* __restrict__ p_in;
     const float2* __restrict__ gamma;
     int64_t ldg;
@@ -91,8 +115,8 @@ struct FwdArgs {
     float2* __restrict__ part;  // [groups][S][B][E]
 };
 
-template <int NC, int KE>
-__global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
+template <int NC, int KE, bool GEN>
+__device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
     const int EB = a.eyb;
@@ -104,7 +128,7 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
     // a block covers EB element rows ey0 .. ey0+EB-1: each staged q line feeds all of them
     const int grp = blockIdx.x / a.n_eyb, ey0 = (blockIdx.x - grp * a.n_eyb) * EB;
     const int neb = min(EB, g.Ey - ey0);
-    const int f = blockIdx.y;
+    const int f = a.f_base + blockIdx.y;
     const int b = blockIdx.z / a.npass, cp = blockIdx.z - b * a.npass;
     const int s0 = a.f_slot_ptr[f];
     const int ns = a.f_slot_ptr[f + 1] - s0;
@@ -148,7 +172,7 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
         __syncthreads();
         for (int k = 0; k < neb; ++k) {
             const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
-            stage_band(sA + k * g.ppx * g.Ni, a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox, g);
+            stage_row<GEN>(sA + k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
         }
         const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg + pt0;
         for (int idx = threadIdx.x; idx < NC * g.Nx; idx += blockDim.x) {
@@ -214,6 +238,26 @@ __global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
         const int64_t o = ((static_cast<int64_t>(grp) * g.S + sSlot[c]) * a.B + b) * g.E + ex + g.Ex * (ey0 + k);
         a.part[o] = sR[(k * g.Ex + ex) * NC + c];
     }
+}
+
+template <int NC, int KE>
+__global__ void __launch_bounds__(512) fwd_dense_kernel(const FwdArgs a) {
+    fwd_dense_body<NC, KE, false>(a);
+}
+
+// Generated table: computing the entries while the accumulators stay live needs more registers than
+// ptxas grants under a 512-thread bound (it settles at 64 and spills).  80 keeps two 384-thread
+// blocks per SM (the 3D matrix array's shape); wider column and window counts get 128.
+template <int NC, int KE>
+__global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_gen_kernel(const FwdArgs a) {
+    fwd_dense_body<NC, KE, true>(a);
+}
+
+// 3D setups read their (stored or streamed) table through the same register ceilings: on the 3D
+// matrix array the forward then runs 4 % faster than under the 512-thread bound (187 vs 195 ms)
+template <int NC, int KE>
+__global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_dense3_kernel(const FwdArgs a) {
+    fwd_dense_body<NC, KE, false>(a);
 }
 
 // G[s][b][e] = sum over line groups of the forward partials
@@ -449,7 +493,9 @@ bool use_mix_tile(const Plan* p, int B) { return B >= 8 && p->E <= kMixEMax; }
 // ---------------------------------------------------------------------------
 struct AdjArgs {
     LineGeom g;
-    const float2* __restrict__ table;
+    const float2* __restrict__ table;  // stored table (frequencies from tab_f0 on), or null when generated (gen)
+    TableGen gen;
+    int fc_base, tab_f0;               // frequency chunk of blockIdx.y = 0; first frequency the table holds
     const float2* __restrict__ p_in;
     const float2* __restrict__ V;   // [S][B][E]
     const int* __restrict__ f_slot_ptr;
@@ -462,8 +508,8 @@ struct AdjArgs {
     float2* __restrict__ part;      // [nfc][B][P]
 };
 
-template <int NC, int KJ>
-__global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
+template <int NC, int KJ, bool GEN>
+__device__ __forceinline__ void adj_dense_body(const AdjArgs& a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
     const int EB = a.eyb;
@@ -477,7 +523,7 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
 
     const int line = blockIdx.x;
     const int iy = line % g.Ny, z = line / g.Ny;
-    const int fc = blockIdx.y, b = blockIdx.z;
+    const int fc = a.fc_base + blockIdx.y, b = blockIdx.z;
     const int64_t pt0 = (static_cast<int64_t>(z) * g.Ny + iy) * g.Nx;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -520,8 +566,7 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
                 if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
                 for (int k = 0; k < neb; ++k) {
                     const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
-                    stage_band(sA + k * g.ppx * g.Ni, a.table + ((static_cast<int64_t>(f) * g.Nz + z) * g.Noy + oy) * g.Nox,
-                               g);
+                    stage_row<GEN>(sA + k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
                 }
                 __syncthreads();
                 for (int idx = threadIdx.x; idx < neb * NC * g.Ex; idx += blockDim.x) {
@@ -601,6 +646,23 @@ __global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
     }
     float2* out = a.part + (static_cast<int64_t>(fc) * a.B + b) * g.P + pt0;
     for (int x = threadIdx.x; x < g.Nx; x += blockDim.x) out[x] = sR[x];
+}
+
+template <int NC, int KJ>
+__global__ void __launch_bounds__(512) adj_dense_kernel(const AdjArgs a) {
+    adj_dense_body<NC, KJ, false>(a);
+}
+
+// Generated table (see fwd_gen_kernel): 112 registers keep three 192-thread blocks per SM.
+template <int NC, int KJ>
+__global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_gen_kernel(const AdjArgs a) {
+    adj_dense_body<NC, KJ, true>(a);
+}
+
+// 3D setups with a stored or streamed table (see fwd_dense3_kernel): 237 vs 246 ms on the 3D array
+template <int NC, int KJ>
+__global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_dense3_kernel(const AdjArgs a) {
+    adj_dense_body<NC, KJ, false>(a);
 }
 
 // gamma_hat[b][p] = sum over frequency chunks
@@ -760,12 +822,33 @@ AdjShape adj_shape(const Plan* p, int kj) {
     return s;
 }
 
+// Streamed table: the rows of frequencies f0 .. f0+nf-1 generated into the plan's chunk buffer
+// (layout [nf][Nz][Noy][Nox], like the stored table).  Block = rows, thread = lateral offset.
+__global__ void __launch_bounds__(256) table_chunk_kernel(const TableGen t, int f0, int n_rows, int Nz, int Noy,
+                                                          float2* __restrict__ out) {
+    for (int row = blockIdx.x; row < n_rows; row += gridDim.x) {
+        const int oy = row % Noy, rz = row / Noy;
+        const GenRow g = gen_row(t, f0 + rz / Nz, rz % Nz, oy);
+        float2* o = out + static_cast<int64_t>(row) * t.Nox;
+        for (int ox = threadIdx.x; ox < t.Nox; ox += blockDim.x) o[ox] = gen_entry(t, g, ox);
+    }
+}
+
+cudaError_t stream_table_chunk(const Plan* p, int f0, int nf, cudaStream_t st) {
+    const int n_rows = nf * p->Nz * p->Noy;
+    const int threads = std::min(256, (p->Nox + 31) / 32 * 32);
+    table_chunk_kernel<<<std::min(n_rows, 152 * 16), threads, 0, st>>>(p->gen, f0, n_rows, p->Nz, p->Noy, p->stream_buf);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <int NC, int KE>
 cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
     const FwdShape sh = fwd_shape(p, KE);
     FwdArgs a;
     a.g = geom_of(p);
-    a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.table = p->table; a.gen = p->gen; a.f_base = 0; a.tab_f0 = 0;
+    a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.lines_per_group = p->fwd_lines_per_group; a.n_lines = p->Ny * p->Nz;
     a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask; a.le = sh.le;
@@ -773,14 +856,25 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = p->ws_part;
     const size_t smem = fwd_smem_bytes(p, NC);
-    cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    void (*kern)(const FwdArgs) = p->table_mode == CUI_STORAGE_GENERATED ? fwd_gen_kernel<NC, KE>
+                                  : p->n_dims == 3                        ? fwd_dense3_kernel<NC, KE>
+                                                                          : fwd_dense_kernel<NC, KE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    dim3 grid(p->fwd_groups * a.n_eyb, p->F, B * a.npass);
     if ((e = timing_begin(const_cast<Plan*>(p), 0, st)) != cudaSuccess) return e;
-    fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
-    count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // streamed table: one chunk of frequencies at a time, generated into the chunk buffer and consumed
+    // by the stored-table kernel before the next chunk overwrites it (stream order)
+    const int fstep = p->table_mode == CUI_STORAGE_STREAMED ? p->stream_nf : p->F;
+    for (int f0 = 0; f0 < p->F; f0 += fstep) {
+        const int nf = std::min(fstep, p->F - f0);
+        if (p->table_mode == CUI_STORAGE_STREAMED) {
+            if ((e = stream_table_chunk(p, f0, nf, st)) != cudaSuccess) return e;
+            a.table = p->stream_buf; a.f_base = f0; a.tab_f0 = f0;
+        }
+        kern<<<dim3(p->fwd_groups * a.n_eyb, nf, B * a.npass), sh.threads, smem, st>>>(a);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     return timing_end(const_cast<Plan*>(p), st);
 }
 
@@ -789,21 +883,36 @@ cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
     const AdjShape sh = adj_shape(p, KJ);
     AdjArgs a;
     a.g = geom_of(p);
-    a.table = p->table; a.p_in = p->p_in; a.V = p->ws_G;
+    a.table = p->table; a.gen = p->gen; a.fc_base = 0; a.tab_f0 = 0;
+    a.p_in = p->p_in; a.V = p->ws_G;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.fchunk = p->adj_fchunk;
     a.n_jg = sh.n_jg; a.nseg_e = sh.nseg_e; a.Es = sh.Es; a.ntask = sh.ntask;
     a.lj = sh.lj; a.nsub = sh.nsub;
     a.B = B; a.eyb = adj_eyb(p); a.part = p->ws_part;
     const size_t smem = adj_smem_bytes(p, NC);
-    cudaError_t e = cudaFuncSetAttribute(adj_dense_kernel<NC, KJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    void (*kern)(const AdjArgs) = p->table_mode == CUI_STORAGE_GENERATED ? adj_gen_kernel<NC, KJ>
+                                  : p->n_dims == 3                        ? adj_dense3_kernel<NC, KJ>
+                                                                          : adj_dense_kernel<NC, KJ>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    dim3 grid(p->Ny * p->Nz, p->adj_nfc, B);
     if ((e = timing_begin(const_cast<Plan*>(p), 1, st)) != cudaSuccess) return e;
-    adj_dense_kernel<NC, KJ><<<grid, sh.threads, smem, st>>>(a);
-    count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (p->table_mode == CUI_STORAGE_STREAMED) {
+        // a streamed plan's frequency chunks are the adjoint's (adj_fchunk == stream_nf): chunk c is
+        // generated, then contracted by the blocks of frequency chunk c
+        for (int c = 0; c < p->adj_nfc; ++c) {
+            const int f0 = c * p->adj_fchunk;
+            if ((e = stream_table_chunk(p, f0, std::min(p->adj_fchunk, p->F - f0), st)) != cudaSuccess) return e;
+            a.table = p->stream_buf; a.fc_base = c; a.tab_f0 = f0;
+            kern<<<dim3(p->Ny * p->Nz, 1, B), sh.threads, smem, st>>>(a);
+            count_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+    } else {
+        kern<<<dim3(p->Ny * p->Nz, p->adj_nfc, B), sh.threads, smem, st>>>(a);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     return timing_end(const_cast<Plan*>(p), st);
 }
 
@@ -1080,7 +1189,8 @@ cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, i
     const FwdShape sh = fwd_shape(p, KE);
     FwdArgs a;
     a.g = geom_of(p);
-    a.table = p->table; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.table = p->table; a.gen = p->gen; a.f_base = 0; a.tab_f0 = 0;
+    a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.lines_per_group = lines_per_group; a.n_lines = p->Ny * p->Nz;
     a.n_eg = sh.n_eg; a.nseg = sh.nseg; a.Js = sh.Js; a.ntask = sh.ntask; a.le = sh.le;
@@ -1088,11 +1198,14 @@ cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, i
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = part;
     const size_t smem = fwd_smem_bytes(p, NC);
-    cudaError_t e = cudaFuncSetAttribute(fwd_dense_kernel<NC, KE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    // a table that is not stored (generated or streamed) is generated inside the kernel here: the
+    // chunk buffer of a streamed plan may be in use by work on another stream
+    void (*kern)(const FwdArgs) = p->table_mode != CUI_STORAGE_STORED ? fwd_gen_kernel<NC, KE>
+                                                                    : fwd_dense_kernel<NC, KE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(groups * a.n_eyb, p->F, B * a.npass);
-    fwd_dense_kernel<NC, KE><<<grid, sh.threads, smem, st>>>(a);
+    kern<<<grid, sh.threads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
 }

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -165,9 +166,10 @@ __global__ void table_kernel(const TableArgs a) {
 struct PinArgs {
     int Nx, Ny, Nz, Ex, Ey, ppx, ppy, Nox, Noy;
     int64_t P;
-    const float2* table;   // transmit table [F][Nz][Noy][Nox]
+    const float2* table;   // transmit table of frequencies f0 .. f0+nf-1: [nf][Nz][Noy][Nox]
     const float2* vd;      // [S][E]
     const int* slot_f;     // [S]
+    int f0, nf;
     float2* p_in;          // [S][P]
 };
 
@@ -178,7 +180,8 @@ __global__ void __launch_bounds__(256) incident_kernel(const PinArgs a) {
     float2* svd = sm + a.Nox;      // [Ex]
     const int line = blockIdx.x, s = blockIdx.y;
     const int iy = line % a.Ny, z = line / a.Ny;
-    const int f = a.slot_f[s];
+    const int f = a.slot_f[s] - a.f0;
+    if (f < 0 || f >= a.nf) return;  // slot of another frequency chunk (uniform over the block)
     const int64_t pt0 = (static_cast<int64_t>(z) * a.Ny + iy) * a.Nx;
     const int x = blockIdx.z * blockDim.x + threadIdx.x;
     float2 acc = make_float2(0.f, 0.f);
@@ -249,9 +252,11 @@ int points_per_pitch(double pitch, double delta, bool* ok) {
 
 #define CUI_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return check_cuda(e_, #x); } while (0)
 
-cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk, double beta, float2* out, int* dbad) {
+// table entries of the nf frequencies whose wavenumbers start at dk, into out [nf][Nz][Noy][Nox]
+cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk, int nf, double beta, float2* out,
+                        int* dbad) {
     TableArgs a;
-    a.n_dims = p.n_dims; a.F = p.F; a.Nz = p.Nz; a.Noy = p.Noy; a.Nox = p.Nox; a.Ex = p.Ex; a.Ey = p.Ey;
+    a.n_dims = p.n_dims; a.F = nf; a.Nz = p.Nz; a.Noy = p.Noy; a.Nox = p.Nox; a.Ex = p.Ex; a.Ey = p.Ey;
     a.Qx = std::max(1, d->n_face_axis[0]);
     a.Qy = (p.n_dims == 3) ? std::max(1, d->n_face_axis[1]) : 1;
     a.dx = d->delta_axis[0];
@@ -267,7 +272,7 @@ cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk
     a.k = dk;
     a.out = out;
     a.bad = dbad;
-    const int64_t n = static_cast<int64_t>(p.F) * p.Nz * p.Noy * p.Nox;
+    const int64_t n = static_cast<int64_t>(nf) * p.Nz * p.Noy * p.Nox;
     const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, 152 * 64));
     table_kernel<<<blocks, 256>>>(a);
     count_launch();
@@ -275,8 +280,99 @@ cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk
     return CUI_OK;
 }
 
-cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan& p, const char* cache_dir,
-                        int32_t* loaded) {
+// Parameters of the generated table (cui_gen.cuh): per frequency the wavenumber with its real part
+// split into an FP32 pair; per lateral offset and face quadrature point the squared distance, and per
+// row the squared depth, computed in FP64 like table_kernel and split into FP32 pairs.
+cui_status build_generator(Plan& p, const cui_born_setup_desc* d, const std::vector<double2>& k) {
+    const int Qx = std::max(1, d->n_face_axis[0]), Qy = std::max(1, d->n_face_axis[1]);
+    const double dx = d->delta_axis[0], dy = d->delta_axis[1], dz = d->delta_axis[2];
+    const double wx = d->width_axis[0], wy = d->width_axis[1];
+    auto split = [](double v) {
+        const float hi = static_cast<float>(v);
+        return make_float2(hi, static_cast<float>(v - static_cast<double>(hi)));
+    };
+    std::vector<float4> fk(p.F);
+    for (int f = 0; f < p.F; ++f) {
+        const float2 kr = split(k[f].x);
+        fk[f] = make_float4(kr.x, kr.y, static_cast<float>(k[f].y), kr.x);
+    }
+    std::vector<float2> sx2(static_cast<size_t>(Qx) * p.Nox), sy2(static_cast<size_t>(Qy) * p.Noy), sz2(p.Nz);
+    std::vector<float> ax(p.Nox), ay(p.Noy);
+    for (int ox = 0; ox < p.Nox; ++ox) {
+        const double X = (ox - 0.5 * (p.Nox - 1)) * dx;
+        ax[ox] = static_cast<float>(std::fabs(X));
+        for (int q = 0; q < Qx; ++q) {
+            const double fx = (q - 0.5 * (Qx - 1)) * (wx / Qx);
+            sx2[static_cast<size_t>(q) * p.Nox + ox] = split((X - fx) * (X - fx));
+        }
+    }
+    for (int oy = 0; oy < p.Noy; ++oy) {
+        const double Y = (oy - 0.5 * (p.Noy - 1)) * dy;
+        ay[oy] = static_cast<float>(std::fabs(Y));
+        for (int q = 0; q < Qy; ++q) {
+            const double fy = (q - 0.5 * (Qy - 1)) * (wy / Qy);
+            sy2[static_cast<size_t>(q) * p.Noy + oy] = split((Y - fy) * (Y - fy));
+        }
+    }
+    for (int z = 0; z < p.Nz; ++z) {
+        const double Z = d->z_start + (z + 0.5) * dz;
+        sz2[z] = split(Z * Z);
+    }
+    cui_status st;
+    auto up = [&](void** dst, const void* src, size_t bytes) -> cui_status {
+        cui_status s2 = device_alloc(p, dst, bytes);
+        if (s2 != CUI_OK) return s2;
+        return check_cuda(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), "generated table parameters");
+    };
+    float4* dfk = nullptr;
+    float2 *dsx = nullptr, *dsy = nullptr, *dsz = nullptr;
+    float *dax = nullptr, *day = nullptr;
+    if ((st = up(reinterpret_cast<void**>(&dfk), fk.data(), sizeof(float4) * fk.size())) != CUI_OK ||
+        (st = up(reinterpret_cast<void**>(&dsx), sx2.data(), sizeof(float2) * sx2.size())) != CUI_OK ||
+        (st = up(reinterpret_cast<void**>(&dsy), sy2.data(), sizeof(float2) * sy2.size())) != CUI_OK ||
+        (st = up(reinterpret_cast<void**>(&dsz), sz2.data(), sizeof(float2) * sz2.size())) != CUI_OK ||
+        (st = up(reinterpret_cast<void**>(&dax), ax.data(), sizeof(float) * ax.size())) != CUI_OK ||
+        (st = up(reinterpret_cast<void**>(&day), ay.data(), sizeof(float) * ay.size())) != CUI_OK)
+        return st;
+    TableGen& t = p.gen;
+    t.fk = dfk; t.sx2 = dsx; t.sy2 = dsy; t.sz2 = dsz; t.ax = dax; t.ay = day;
+    t.Nox = p.Nox; t.Noy = p.Noy; t.Qx = Qx; t.Qy = Qy;
+    t.scale = static_cast<float>((wx / Qx) * (wy / Qy) / (2.0 * kPi));  // -2 dA * (-1 / (4 pi))
+    t.pitch_x = static_cast<float>(d->pitch_axis[0]);
+    t.pitch_y = static_cast<float>(d->pitch_axis[1]);
+    const double beta = d->aa_rx_beta;
+    t.win_x = (beta >= 0.0 && p.Ex > 1) ? 1 : 0;
+    t.win_y = (beta >= 0.0 && p.Ey > 1) ? 1 : 0;
+    t.lb = static_cast<float>(kPi * (1.0 - beta));
+    t.inv_span = beta > 0.0 ? static_cast<float>(1.0 / (kPi * beta)) : 0.f;  // beta = 0: no transition band
+    return CUI_OK;
+}
+
+// transmit-table chunks of a plan whose table is not stored (and of a stored plan whose two
+// filters differ)
+constexpr size_t kTxChunkBytes = size_t(1) << 30;
+// chunk buffer of a streamed table, and the adjoint partial sums that its frequency chunks need
+constexpr size_t kStreamBytes = size_t(512) << 20;
+constexpr size_t kStreamPartBytes = size_t(1) << 30;
+
+// Frequencies per streamed chunk: what fits the chunk buffer, capped by CUI_BORN_STREAM_FREQUENCIES,
+// but no more chunks than the adjoint's partial sums (one slab of max_objects x P per chunk) allow;
+// and no more frequencies than the adjoint already takes per block.  The adjoint's frequency chunks
+// become the streamed chunks.
+int stream_frequencies(const Plan& p, size_t fbytes) {
+    int nf = static_cast<int>(std::max<size_t>(1, std::min<size_t>(p.F, kStreamBytes / fbytes)));
+    if (const char* env = std::getenv("CUI_BORN_STREAM_FREQUENCIES")) {
+        const int cap = std::atoi(env);
+        if (cap > 0) nf = std::min(nf, cap);
+    }
+    const size_t slab = sizeof(float2) * static_cast<size_t>(p.max_objects) * p.P;
+    const int max_chunks = static_cast<int>(std::max<size_t>(1, kStreamPartBytes / slab));
+    nf = std::max(nf, (p.F + max_chunks - 1) / max_chunks);
+    return std::max(1, std::min(nf, p.adj_fchunk));
+}
+
+cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32_t storage, Plan& p,
+                        const char* cache_dir, int32_t* loaded) {
     if (!d) return set_error(CUI_ERR_INVALID_ARG, "desc is NULL");
     if (d->n_dims != 2 && d->n_dims != 3) return set_error(CUI_ERR_INVALID_ARG, "n_dims must be 2 or 3");
     const int nl = d->n_dims - 1;
@@ -341,18 +437,46 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
         return e;
     };
     cudaError_t ce;
-    const size_t tbytes = sizeof(float2) * static_cast<size_t>(p.F) * p.Nz * p.Noy * p.Nox;
-    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.table), tbytes)) != CUI_OK) return st;
-    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_in), sizeof(float2) * static_cast<size_t>(p.S) * p.P)) != CUI_OK)
-        return st;
-    p.table_bytes = tbytes;
-    p.incident_bytes = sizeof(float2) * static_cast<size_t>(p.S) * p.P;
-    // compute_or_load_hash.m:65-185: load both arrays from the cache file of this setup if it exists
+    const size_t fbytes = sizeof(float2) * static_cast<size_t>(p.Nz) * p.Noy * p.Nox;  // one frequency
+    const size_t tbytes = fbytes * p.F;
+    const size_t ibytes = sizeof(float2) * static_cast<size_t>(p.S) * p.P;
+    int mode = storage;
+    const int stream_nf = stream_frequencies(p, fbytes);
+    if (mode == CUI_STORAGE_AUTO) {
+        mode = CUI_STORAGE_STORED;
+        size_t free_b = 0, total_b = 0;
+        if (p.n_dims == 3 && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && tbytes + ibytes > free_b / 10 * 9)
+            mode = (fbytes * stream_nf + ibytes <= free_b / 10 * 9) ? CUI_STORAGE_STREAMED : CUI_STORAGE_GENERATED;
+    } else if (mode != CUI_STORAGE_STORED && mode != CUI_STORAGE_GENERATED && mode != CUI_STORAGE_STREAMED) {
+        return set_error(CUI_ERR_INVALID_ARG, "unknown table storage");
+    }
+    if (mode != CUI_STORAGE_STORED && p.n_dims != 3)
+        return set_error(CUI_ERR_UNSUPPORTED_SETUP, "a streamed or generated table needs a 3D setup (2D entries are "
+                                                    "Hankel functions: too costly to recompute per apply)");
+    p.table_mode = mode;
+    if (mode == CUI_STORAGE_STORED) {
+        if ((st = device_alloc(p, reinterpret_cast<void**>(&p.table), tbytes)) != CUI_OK) return st;
+        p.table_bytes = tbytes;
+    } else {
+        if ((st = build_generator(p, d, k)) != CUI_OK) return st;
+        p.table_bytes = 0;
+        if (mode == CUI_STORAGE_STREAMED) {
+            p.stream_nf = stream_nf;
+            p.adj_fchunk = stream_nf;  // the adjoint's frequency chunks are the streamed chunks
+            p.adj_nfc = (p.F + stream_nf - 1) / stream_nf;
+            p.table_bytes = fbytes * stream_nf;
+            if ((st = device_alloc(p, reinterpret_cast<void**>(&p.stream_buf), p.table_bytes)) != CUI_OK) return st;
+        }
+    }
+    if ((st = device_alloc(p, reinterpret_cast<void**>(&p.p_in), ibytes)) != CUI_OK) return st;
+    p.incident_bytes = ibytes;
+    // compute_or_load_hash.m:65-185: load the arrays from the cache file of this setup if it exists
+    // (a generated plan keeps only the incident fields, in a file of its own)
     std::vector<unsigned char> key;
     std::string path;
     if (cache_dir) {
         if ((st = setup_key(d, key)) != CUI_OK) return st;
-        path = cache_path(cache_dir, key);
+        path = cache_path(cache_dir, key, mode != CUI_STORAGE_STORED);
         bool hit = false;
         if ((st = cache_load(path, key, p, &hit)) != CUI_OK) return st;
         if (hit) {
@@ -361,11 +485,15 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
         }
     }
     const bool same_filter = (d->aa_tx_beta < 0.0 && d->aa_rx_beta < 0.0) || (d->aa_tx_beta == d->aa_rx_beta);
+    // the transmit table is the stored table itself when both filters agree; else it is built in
+    // chunks of frequencies into scratch, each chunk consumed by the incident-field kernel
+    const bool own_tx = mode != CUI_STORAGE_STORED || !same_filter;
+    const int fchunk = own_tx ? static_cast<int>(std::max<size_t>(1, std::min<size_t>(p.F, kTxChunkBytes / fbytes))) : p.F;
     if ((ce = talloc(reinterpret_cast<void**>(&dk), sizeof(double2) * p.F)) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dvd), sizeof(float2) * vd.size())) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dslot), sizeof(int) * p.S)) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dbad), sizeof(int))) != cudaSuccess ||
-        (!same_filter && (ce = talloc(reinterpret_cast<void**>(&dtx), tbytes)) != cudaSuccess)) {
+        (own_tx && (ce = talloc(reinterpret_cast<void**>(&dtx), fbytes * fchunk)) != cudaSuccess)) {
         release();
         return check_cuda(ce, "table build scratch");
     }
@@ -377,14 +505,16 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
         return check_cuda(ce, "table build upload");
     }
     std::vector<float2>().swap(vd);
-    st = launch_table(p, d, dk, d->aa_rx_beta, p.table, dbad);
-    if (st == CUI_OK && !same_filter) st = launch_table(p, d, dk, d->aa_tx_beta, dtx, dbad);
-    if (st == CUI_OK) {
+    if (mode == CUI_STORAGE_STORED) st = launch_table(p, d, dk, p.F, d->aa_rx_beta, p.table, dbad);
+    for (int f0 = 0; st == CUI_OK && f0 < p.F; f0 += fchunk) {
+        const int nf = std::min(fchunk, p.F - f0);
+        if (own_tx) st = launch_table(p, d, dk + f0, nf, d->aa_tx_beta, dtx, dbad);
+        if (st != CUI_OK) break;
         PinArgs a;
         a.Nx = p.Nx; a.Ny = p.Ny; a.Nz = p.Nz; a.Ex = p.Ex; a.Ey = p.Ey; a.ppx = p.ppx; a.ppy = p.ppy;
         a.Nox = p.Nox; a.Noy = p.Noy; a.P = p.P;
-        a.table = same_filter ? p.table : dtx;
-        a.vd = dvd; a.slot_f = dslot; a.p_in = p.p_in;
+        a.table = own_tx ? dtx : p.table;
+        a.vd = dvd; a.slot_f = dslot; a.f0 = f0; a.nf = nf; a.p_in = p.p_in;
         const size_t smem = sizeof(float2) * (p.Nox + p.Ex);
         const int tpb = 256;
         dim3 grid(p.Ny * p.Nz, p.S, (p.Nx + tpb - 1) / tpb);
@@ -414,15 +544,15 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, Plan&
 }  // namespace cui
 
 namespace {
-cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_objects, const char* cache_dir,
-                             int32_t* loaded, cui_born_plan** plan) {
+cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_objects, int32_t storage,
+                             const char* cache_dir, int32_t* loaded, cui_born_plan** plan) {
     if (!plan) return cui::set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     *plan = nullptr;
     cui_born_plan* h = new (std::nothrow) cui_born_plan();
     if (!h) return cui::set_error(CUI_ERR_OOM, "host allocation failed");
     cui_status s;
     try {
-        s = cui::create_setup(desc, max_objects, h->p, cache_dir, loaded);
+        s = cui::create_setup(desc, max_objects, storage, h->p, cache_dir, loaded);
     } catch (const std::bad_alloc&) {
         s = cui::set_error(CUI_ERR_OOM, "host allocation failed");
     }
@@ -437,12 +567,25 @@ cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_object
 
 extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
                                                  cui_born_plan** plan) {
-    return create_setup_plan(desc, max_objects, nullptr, nullptr, plan);
+    return create_setup_plan(desc, max_objects, CUI_STORAGE_AUTO, nullptr, nullptr, plan);
+}
+
+extern "C" cui_status cui_born_plan_create_setup_ex(const cui_born_setup_desc* desc, int32_t max_objects,
+                                                    int32_t storage, const char* cache_dir, cui_born_plan** plan,
+                                                    int32_t* loaded) {
+    if (loaded) *loaded = 0;
+    return create_setup_plan(desc, max_objects, storage, cache_dir, loaded, plan);
+}
+
+extern "C" cui_status cui_born_plan_table_storage(const cui_born_plan* plan, int32_t* storage) {
+    if (!plan || !storage) return cui::set_error(CUI_ERR_INVALID_ARG, "plan or storage is NULL");
+    *storage = plan->p.table_mode;
+    return CUI_OK;
 }
 
 extern "C" cui_status cui_born_plan_create_setup_cached(const cui_born_setup_desc* desc, int32_t max_objects,
                                                         const char* cache_dir, cui_born_plan** plan, int32_t* loaded) {
     if (!cache_dir) return cui::set_error(CUI_ERR_INVALID_ARG, "cache_dir is NULL");
     if (loaded) *loaded = 0;
-    return create_setup_plan(desc, max_objects, cache_dir, loaded, plan);
+    return create_setup_plan(desc, max_objects, CUI_STORAGE_AUTO, cache_dir, loaded, plan);
 }

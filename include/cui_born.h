@@ -188,6 +188,42 @@ cui_status cui_born_plan_create_setup_cached(const cui_born_setup_desc* desc, in
  * velocities; not the receive mixes or the device -- as 16 hex digits and a
  * NUL in `hex17`.  Host only (no GPU). */
 cui_status cui_born_setup_hash(const cui_born_setup_desc* desc, char* hex17);
+/* Storage of the lateral transfer-function table of a setup-form plan (no
+ * counterpart in the reference, which always holds h_ref: operator.m:76-88).
+ *   CUI_STORAGE_STORED: built once at creation ([F][Nz][Noy][Nox] FP32), read by
+ *     every apply.
+ *   CUI_STORAGE_STREAMED (3D setups): never stored whole; every apply regenerates
+ *     it one chunk of frequencies at a time into a chunk buffer (about 512 MiB;
+ *     the environment variable CUI_BORN_STREAM_FREQUENCIES caps the frequencies
+ *     per chunk) that the contraction kernels read before the next chunk
+ *     replaces it.  table_bytes is the buffer's size.
+ *   CUI_STORAGE_GENERATED (3D setups): never stored at all; the contraction and
+ *     received-energy kernels compute each entry where they stage it.  No table
+ *     memory (table_bytes 0), at about 1.5x the apply time of the other two.
+ * Generated entries are formed in FP32 with the distance and the phase range
+ * reduction in FP32 pairs (relative entry error below 1e-6; the stored table is
+ * computed in FP64 and rounded to FP32).  Streamed and generated plans run the
+ * FP32 CUDA-core kernels only (cui_born_set_precision(BF16X3) is
+ * CUI_ERR_UNSUPPORTED_SETUP); their received energies and
+ * cui_born_forward_static generate the entries in the kernel.  Their incident
+ * fields are stored, built from transmit-table chunks of a few frequencies.
+ *   CUI_STORAGE_AUTO: stored, unless the table and the incident fields would not
+ *     fit in the device's free memory; then streamed (3D; generated if not even
+ *     the chunk buffer fits) or CUI_ERR_OOM (2D).
+ * cui_born_plan_create_setup uses CUI_STORAGE_AUTO. */
+typedef enum {
+    CUI_STORAGE_AUTO = 0,
+    CUI_STORAGE_STORED = 1,
+    CUI_STORAGE_GENERATED = 2,
+    CUI_STORAGE_STREAMED = 3
+} cui_table_storage;
+/* `cache_dir` (may be NULL) and `loaded` (may be NULL) as in
+ * cui_born_plan_create_setup_cached; a streamed or generated plan caches only
+ * the incident fields, in `cache_dir`/cui_born_<hash>.incident. */
+cui_status cui_born_plan_create_setup_ex(const cui_born_setup_desc* desc, int32_t max_objects, int32_t storage,
+                                         const char* cache_dir, cui_born_plan** plan, int32_t* loaded);
+/* The storage a plan uses (CUI_STORAGE_STORED, _STREAMED or _GENERATED). */
+cui_status cui_born_plan_table_storage(const cui_born_plan* plan, int32_t* storage);
 cui_status cui_born_plan_destroy(cui_born_plan* plan);
 cui_status cui_born_plan_info(const cui_born_plan* plan, cui_born_info* info);
 

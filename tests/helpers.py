@@ -8,8 +8,9 @@ from oracle import configs
 
 
 def rel_l2(x, ref) -> float:
-    x = np.asarray(x)
-    ref = np.asarray(ref)
+    # in double precision: the squares of FP32 values such as received energies (~1e-26) underflow
+    x = np.asarray(x).astype(np.complex128)
+    ref = np.asarray(ref).astype(np.complex128)
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
 
 

@@ -7,7 +7,7 @@ hold at any size (the FP64 oracle would take hours there):
 
 Every call goes through the C-ABI (ctypes mirror), on the path each workload
 benchmarks: split-BF16 tensor cores for the 2D workloads (and FP32 beside
-them), FP32 for the 3D matrix array.
+them), FP32 for the 3D matrix array, with its table stored, streamed and generated.
 """
 
 import numpy as np
@@ -26,19 +26,22 @@ def _rand(shape, gen):
     return torch.complex(re, im)
 
 
-@pytest.mark.parametrize("wname,precision,n_obj", [
-    ("2d-batched", "bf16x3", 64),
-    ("2d-batched", "fp32", 4),
-    ("2d-gradient", "bf16x3", 1),
-    ("2d-gradient", "fp32", 1),
-    ("3d", "fp32", 1),
+@pytest.mark.parametrize("wname,precision,n_obj,storage", [
+    ("2d-batched", "bf16x3", 64, "stored"),
+    ("2d-batched", "fp32", 4, "stored"),
+    ("2d-gradient", "bf16x3", 1, "stored"),
+    ("2d-gradient", "fp32", 1, "stored"),
+    ("3d", "fp32", 1, "stored"),
+    ("3d", "fp32", 1, "streamed"),
+    ("3d", "fp32", 1, "generated"),
 ])
-def test_full_size_adjointness_and_linearity(wname, precision, n_obj):
+def test_full_size_adjointness_and_linearity(wname, precision, n_obj, storage):
     from comp_ui_toolbox_gb300 import OperatorBorn
     from comp_ui_toolbox_gb300.workloads import workload
 
     w = workload(wname)
-    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj, table_storage=storage)
+    assert op.table_storage == storage
     op.set_precision(precision)
     gen = torch.Generator(device="cuda").manual_seed(1234)
     x1 = _rand((op.n_points, n_obj), gen)

@@ -1,0 +1,172 @@
+"""Lateral table not stored (3D setups): ``table_storage="generated"`` -- the contraction
+and received-energy kernels compute every table entry where they stage it -- and
+``"streamed"`` -- every apply regenerates the table one chunk of frequencies at a
+time into a chunk buffer that the stored-table kernels read.  No
+[F][Nz][Noy][Nox] table is held in either.
+
+Checked on seeded 3D setups that cover one and several face quadrature points,
+anti-aliasing on and off, different transmit and receive filters (the incident
+fields then come from transmit-table chunks), 3 and 4 grid points per pitch and
+5-8 waves per frequency:
+
+- forward, adjoint, VJP and energy_rx against the FP64 oracle, relative L2 <= 1e-5
+  (the bound of every FP32 parity test of this library);
+- the same applies against the stored-table plan of the same setup, relative
+  L2 <= 2e-6: the generator's FP32 entries differ from the stored FP32 entries
+  (FP64 arithmetic, rounded) by less than 1e-6 relative;
+- the small setups stream one frequency per chunk (several chunks per apply);
+- the allocation-free forward (cui_born_forward_static) of both;
+- the table cache of both holds only the incident fields;
+- refusals: a 2D setup, the tensor-core path.
+"""
+
+import dataclasses
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import adjoint_quick_cpu, configs, forward_quick_cpu
+from oracle.born_oracle import Absorption, energy_rx_cpu
+from tests.helpers import rel_l2, setup_kwargs
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5        # relative L2 vs the FP64 oracle
+TOL_STORED = 2e-6  # relative L2 vs the stored-table plan of the same setup
+
+
+def _cases():
+    base = configs.small_config("c3")
+    s = base.setup
+    quad = dataclasses.replace(s, n_face_axis=(2, 2), aa_rx_beta=0.3, aa_tx_beta=None,
+                               absorption=Absorption("none", 1540.0))
+    wide = dataclasses.replace(s, n_points_axis=(20, 9, 5), delta_axis=(1e-4, 1.5e-4, 1e-4), z_start=2e-3,
+                               n_elements_axis=(5, 4), pitch_axis=(4e-4, 3e-4), width_axis=(3.6e-4, 2.7e-4),
+                               aa_rx_beta=None, aa_tx_beta=0.5)
+    return {
+        "c3-small": base,
+        "quadrature": dataclasses.replace(base, name="quadrature", setup=quad, n_objects=2),
+        "wide-8-waves": dataclasses.replace(
+            base, name="wide-8-waves", setup=wide, n_objects=3,
+            waves=[configs.Wave("qpw", (a, b)) for a, b in ((-9, 0), (-6, 3), (-3, 0), (0, 0), (3, -3),
+                                                             (6, 0), (9, 3), (0, 6))]),
+    }
+
+
+CASES = _cases()
+_BUILT = {}
+
+
+def built(name):
+    if name not in _BUILT:
+        _BUILT[name] = configs.build(CASES[name])
+    return _BUILT[name]
+
+
+def dev(x):
+    return torch.from_numpy(np.asarray(x, dtype=np.complex64)).cuda()
+
+
+STORAGE = ["generated", "streamed"]
+
+
+def _plans(b, B, storage):
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    gen = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B, table_storage=storage)
+    sto = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B, table_storage="stored")
+    assert gen.table_storage == storage and sto.table_storage == "stored"
+    if storage == "generated":
+        assert gen.info["table_bytes"] == 0
+    else:  # one frequency's rows per chunk at these sizes
+        assert 0 < gen.info["table_bytes"] < sto.info["table_bytes"]
+    return gen, sto
+
+
+@pytest.mark.parametrize("storage", STORAGE)
+@pytest.mark.parametrize("name", list(CASES))
+def test_generated_table_matches_oracle_and_stored(name, storage):
+    b = built(name)
+    B = max(1, b.cfg.n_objects)
+    gen, sto = _plans(b, B, storage)
+    gamma = configs.make_gamma(b.cfg, n_objects=B, complex_values=True)
+    u = gen.forward(dev(gamma)).cpu().numpy()
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= TOL
+    assert rel_l2(u, sto.forward(dev(gamma)).cpu().numpy()) <= TOL_STORED
+    rng = np.random.default_rng(31)
+    y = rng.standard_normal((b.op.n_observations, B)) + 1j * rng.standard_normal((b.op.n_observations, B))
+    g = gen.adjoint(dev(y)).cpu().numpy()
+    assert rel_l2(g, adjoint_quick_cpu(b.op, y)) <= TOL
+    assert rel_l2(g, sto.adjoint(dev(y)).cpu().numpy()) <= TOL_STORED
+    E = gen.energy_rx().cpu().numpy()
+    assert rel_l2(E, energy_rx_cpu(b.op)) <= TOL
+    assert rel_l2(E, sto.energy_rx().cpu().numpy()) <= TOL_STORED
+    assert gen.device_status() == 0
+    gen.close()
+    sto.close()
+
+
+@pytest.mark.parametrize("storage", STORAGE)
+def test_generated_table_vjp_matches_oracle(storage):
+    b = built("c3-small")
+    gen, sto = _plans(b, 1, storage)
+    gamma_true = configs.make_gamma(b.cfg)
+    u_meas = configs.add_noise(forward_quick_cpu(b.op, gamma_true), 30.0, seed=5)
+    gamma = np.random.default_rng(21).standard_normal(gamma_true.shape)
+    r = forward_quick_cpu(b.op, gamma) - u_meas
+    grad, loss = gen.vjp(dev(gamma), dev(u_meas))
+    assert rel_l2(grad.cpu().numpy(), adjoint_quick_cpu(b.op, r)) <= TOL
+    assert abs(float(loss[0]) - 0.5 * float(np.vdot(r, r).real)) <= TOL * 0.5 * float(np.vdot(r, r).real)
+    gen.close()
+    sto.close()
+
+
+@pytest.mark.parametrize("storage", STORAGE)
+def test_generated_table_static_forward(storage):
+    b = built("quadrature")
+    B = b.cfg.n_objects
+    gen, sto = _plans(b, B, storage)
+    g = dev(configs.make_gamma(b.cfg, n_objects=B, complex_values=True))
+    gc = g.t().contiguous()
+    out = torch.empty((B, gen.n_observations), dtype=torch.complex64, device="cuda")
+    st = gen._lib.cui_born_forward_static(gen._plan, gc.data_ptr(), gen.n_points, B, out.data_ptr(),
+                                          gen.n_observations, torch.cuda.current_stream().cuda_stream)
+    assert st == 0, gen._lib.cui_last_error()
+    assert rel_l2(out.t().cpu().numpy(), gen.forward(g).cpu().numpy()) <= 1e-6
+    gen.close()
+    sto.close()
+
+
+@pytest.mark.parametrize("storage", STORAGE)
+def test_generated_table_cache_holds_incident_fields(tmp_path: Path, storage):
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.born import setup_hash
+    b = built("c3-small")
+    kw = setup_kwargs(b.cfg)
+    h = setup_hash(**kw)
+    first = OperatorBorn.from_setup(**kw, cache_dir=tmp_path, table_storage=storage)
+    assert first.loaded_from_cache == 0 and first.table_storage == storage
+    assert (tmp_path / f"cui_born_{h}.incident").exists()
+    assert not (tmp_path / f"cui_born_{h}.tables").exists()
+    again = OperatorBorn.from_setup(**kw, cache_dir=tmp_path, table_storage=storage)
+    assert again.loaded_from_cache == 1
+    g = dev(configs.make_gamma(b.cfg))
+    assert torch.equal(first.forward(g), again.forward(g))
+    stored = OperatorBorn.from_setup(**kw, cache_dir=tmp_path, table_storage="stored")
+    assert stored.loaded_from_cache == 0 and (tmp_path / f"cui_born_{h}.tables").exists()
+    for op in (first, again, stored):
+        op.close()
+
+
+@pytest.mark.parametrize("storage", STORAGE)
+def test_generated_table_refusals(storage):
+    from comp_ui_toolbox_gb300 import CuiError, OperatorBorn
+    with pytest.raises(CuiError) as ei:
+        OperatorBorn.from_setup(**setup_kwargs(configs.small_config("c1")), table_storage=storage)
+    assert ei.value.status == 2  # CUI_ERR_UNSUPPORTED_SETUP: 2D entries are Hankel functions
+    gen = OperatorBorn.from_setup(**setup_kwargs(built("c3-small").cfg), table_storage=storage)
+    with pytest.raises(CuiError) as ei:
+        gen.set_precision("bf16x3")
+    assert ei.value.status == 2
+    gen.close()
