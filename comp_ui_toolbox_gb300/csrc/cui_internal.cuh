@@ -88,6 +88,8 @@ struct Plan {
     int n_egroups = 0;
     int* egroup_ptr = nullptr;      // [n_egroups + 1]
     int* egroup_slots = nullptr;    // [S], the first slot of a group is its representative
+    int* egroup_term_ptr = nullptr; // [n_egroups + 1] CSR of the representative's energy terms
+    float4* egroup_terms = nullptr; // (pref re, pref im, bits of (table-row offset << 1 | row end), 0)
 
     // workspace (sized for max_objects at creation; shared by all applies)
     float2* ws_part = nullptr;      // forward / adjoint partial sums

@@ -391,6 +391,35 @@ static void energy_groups(const Plan& p, const HostMeta& h, std::vector<int>& gp
     }
 }
 
+// The terms of ||Phi e_p||^2 for each energy group's representative slot, in the order the energy
+// kernel adds them: per observation row of the slot, per active element a, the element's table-row
+// offset in the staged rows [E_y][N_ox] (e_y N_ox + (E_x - 1 - e_x) ppx) and the prefactor
+// pref[mix][fl, a], packed as (re, im, bits of (offset << 1 | last term of the row), 0).
+static void energy_terms(const Plan& p, const HostMeta& h, const std::vector<int>& gptr,
+                         const std::vector<int>& gslots, std::vector<int>& tptr, std::vector<float4>& terms) {
+    tptr.assign(1, 0);
+    terms.clear();
+    for (size_t g = 0; g + 1 < gptr.size(); ++g) {
+        const int rep = gslots[gptr[g]];
+        for (int rr = h.slot_row_ptr[rep]; rr < h.slot_row_ptr[rep + 1]; ++rr) {
+            const int row = h.slot_rows[rr];
+            const int m = h.row_mix[row], fl = h.row_fl[row];
+            const int nact = h.mix_nact[m], nf = h.mix_nf[m];
+            for (int ia = 0; ia < nact; ++ia) {
+                const int e = h.act[h.mix_act_off[m] + ia];
+                const int ey = p.Ey == 1 ? 0 : e / p.Ex, ex = e - ey * p.Ex;
+                const int toff = ey * p.Nox + (p.Ex - 1 - ex) * p.ppx;
+                const float2 w = h.pref[h.mix_pref_off[m] + static_cast<int64_t>(ia) * nf + fl];
+                const int info = (toff << 1) | (ia == nact - 1 ? 1 : 0);
+                float bits;
+                std::memcpy(&bits, &info, sizeof bits);
+                terms.push_back(make_float4(w.x, w.y, bits, 0.f));
+            }
+        }
+        tptr.push_back(static_cast<int>(terms.size()));
+    }
+}
+
 cui_status upload_metadata_and_workspace(Plan& p) {
     HostMeta& h = p.h_meta;
     CUI_TRY(upload(p, &p.f_slot_ptr, p.h_f_slot_ptr));
@@ -412,6 +441,11 @@ cui_status upload_metadata_and_workspace(Plan& p) {
         std::vector<int> gptr, gslots;
         energy_groups(p, h, gptr, gslots);
         p.n_egroups = static_cast<int>(gptr.size()) - 1;
+        std::vector<int> tptr;
+        std::vector<float4> terms;
+        energy_terms(p, h, gptr, gslots, tptr, terms);
+        CUI_TRY(upload(p, &p.egroup_term_ptr, tptr));
+        CUI_TRY(upload(p, &p.egroup_terms, terms));
         CUI_TRY(upload(p, &p.egroup_ptr, gptr));
         CUI_TRY(upload(p, &p.egroup_slots, gslots));
     }
