@@ -254,7 +254,9 @@ __global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_gen_kernel(const FwdAr
 }
 
 // 3D setups read their (stored or streamed) table through the same register ceilings: on the 3D
-// matrix array the forward then runs 4 % faster than under the 512-thread bound (187 vs 195 ms)
+// matrix array the forward then runs 4 % faster than under the 512-thread bound (187 vs 195 ms).
+// 2D setups take them where the ceiling is 128 (wide column and window counts): 2d-batched FP32
+// forward 891 -> 875 ms; narrower 2D shapes keep the 512-thread bound.
 template <int NC, int KE>
 __global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_dense3_kernel(const FwdArgs a) {
     fwd_dense_body<NC, KE, false>(a);
@@ -659,7 +661,9 @@ __global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_gen_kernel(const AdjA
     adj_dense_body<NC, KJ, true>(a);
 }
 
-// 3D setups with a stored or streamed table (see fwd_dense3_kernel): 237 vs 246 ms on the 3D array
+// 3D setups with a stored or streamed table (see fwd_dense3_kernel): 237 vs 246 ms on the 3D array.
+// 2D setups where the ceiling is 128: 2d-batched FP32 adjoint 802 -> 713 ms, 2d-gradient 14.4 -> 13.2
+// ms; the single-wave 2d-plain adjoint is slower under a ceiling (0.28 -> 0.36 ms) and keeps the bound.
 template <int NC, int KJ>
 __global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_dense3_kernel(const AdjArgs a) {
     adj_dense_body<NC, KJ, false>(a);
@@ -857,7 +861,7 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
     a.part = p->ws_part;
     const size_t smem = fwd_smem_bytes(p, NC);
     void (*kern)(const FwdArgs) = p->table_mode == CUI_STORAGE_GENERATED ? fwd_gen_kernel<NC, KE>
-                                  : p->n_dims == 3                        ? fwd_dense3_kernel<NC, KE>
+                                  : p->n_dims == 3 || NC * KE >= 16       ? fwd_dense3_kernel<NC, KE>
                                                                           : fwd_dense_kernel<NC, KE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
@@ -892,7 +896,7 @@ cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
     a.B = B; a.eyb = adj_eyb(p); a.part = p->ws_part;
     const size_t smem = adj_smem_bytes(p, NC);
     void (*kern)(const AdjArgs) = p->table_mode == CUI_STORAGE_GENERATED ? adj_gen_kernel<NC, KJ>
-                                  : p->n_dims == 3                        ? adj_dense3_kernel<NC, KJ>
+                                  : p->n_dims == 3 || NC * KJ >= 24       ? adj_dense3_kernel<NC, KJ>
                                                                           : adj_dense_kernel<NC, KJ>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
