@@ -96,8 +96,6 @@ struct Plan {
     size_t ws_part_bytes = 0;
     float2* ws_G = nullptr;         // [S][B][E] element signals / unmixed data
     float2* ws_r = nullptr;         // [B][n_obs] residual of the VJP
-    int* ws_occ = nullptr;          // [P] occupied points (sparse forward)
-    int* ws_occ_count = nullptr;    // [2] occupied-point count, spare
     float* ws_loss = nullptr;       // [B] loss partial sums
 
     // launch geometry chosen at creation
