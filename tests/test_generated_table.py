@@ -74,6 +74,9 @@ STORAGE = ["generated", "streamed"]
 
 def _plans(b, B, storage):
     from comp_ui_toolbox_gb300 import OperatorBorn
+    auto = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B)
+    assert auto.table_storage == "stored"  # CUI_STORAGE_AUTO: the small table fits
+    auto.close()
     gen = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B, table_storage=storage)
     sto = OperatorBorn.from_setup(**setup_kwargs(b.cfg), max_objects=B, table_storage="stored")
     assert gen.table_storage == storage and sto.table_storage == "stored"
