@@ -558,7 +558,8 @@ class OperatorBorn:
         lam = 0.0
         for _ in range(n_iter):
             y = self.adjoint(self.forward(x))
-            lam = float(y.norm())
+            # in FP64: the squares of a small operator's entries (3D setups: |Phi^H Phi x| ~ 1e-25) underflow FP32
+            lam = float(torch.linalg.vector_norm(y.to(torch.complex128)))
             x = y / lam
         return lam
 

@@ -94,7 +94,8 @@ __global__ void argmax_final_kernel(const float* __restrict__ bval, const int64_
 }
 
 struct ColumnArgs {
-    const float2* table;
+    const float2* table;  // stored table, or null: entries generated (streamed and generated 3D tables)
+    TableGen gen;
     const float2* p_in;
     const int* slot_f;
     const int* row_slot;
@@ -139,7 +140,8 @@ __global__ void column_kernel(const ColumnArgs a) {
             const int e = act[ia];
             const int ey = e / a.Ex, ex = e - ey * a.Ex;
             const int ox = ix + (a.Ex - 1 - ex) * a.ppx, oy = iy + (a.Ey - 1 - ey) * a.ppy;
-            const float2 h = a.table[((static_cast<int64_t>(f) * a.Nz + iz) * a.Noy + oy) * a.Nox + ox];
+            const float2 h = a.table ? a.table[((static_cast<int64_t>(f) * a.Nz + iz) * a.Noy + oy) * a.Nox + ox]
+                                     : gen_entry(a.gen, gen_row(a.gen, f, iz, oy), ox);
             const float2 w = pref[static_cast<int64_t>(ia) * nf];
             acc.x = fmaf(w.x, h.x, fmaf(-w.y, h.y, acc.x));
             acc.y = fmaf(w.x, h.y, fmaf(w.y, h.x, acc.y));
@@ -321,7 +323,7 @@ __global__ void mag2_kernel(const float2* __restrict__ g, int64_t n, float* __re
 
 ColumnArgs column_args(const Plan& p) {
     ColumnArgs ca{};
-    ca.table = p.table; ca.p_in = p.p_in; ca.slot_f = p.slot_f; ca.row_slot = p.row_slot; ca.row_mix = p.row_mix;
+    ca.table = p.table; ca.gen = p.gen; ca.p_in = p.p_in; ca.slot_f = p.slot_f; ca.row_slot = p.row_slot; ca.row_mix = p.row_mix;
     ca.row_fl = p.row_fl; ca.mix_nact = p.mix_nact; ca.mix_nf = p.mix_nf; ca.mix_act_off = p.mix_act_off;
     ca.mix_pref_off = p.mix_pref_off; ca.act = p.act; ca.pref = p.pref;
     ca.Nx = p.Nx; ca.Ny = p.Ny; ca.Nz = p.Nz; ca.Ex = p.Ex; ca.Ey = p.Ey; ca.ppx = p.ppx; ca.ppy = p.ppy;
