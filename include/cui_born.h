@@ -204,8 +204,9 @@ cui_status cui_born_setup_hash(const cui_born_setup_desc* desc, char* hex17);
  * reduction in FP32 pairs (relative entry error below 1e-6; the stored table is
  * computed in FP64 and rounded to FP32).  Streamed and generated plans run the
  * FP32 CUDA-core kernels only (cui_born_set_precision(BF16X3) is
- * CUI_ERR_UNSUPPORTED_SETUP); their received energies and
- * cui_born_forward_static generate the entries in the kernel.  Their incident
+ * CUI_ERR_UNSUPPORTED_SETUP); their received energies, the Phi columns of
+ * cui_born_omp / cui_born_cosamp and cui_born_forward_static generate the
+ * entries in the kernel.  Their incident
  * fields are stored, built from transmit-table chunks of a few frequencies.
  *   CUI_STORAGE_AUTO: stored, unless the table and the incident fields would not
  *     fit in the device's free memory; then streamed (3D; generated if not even
