@@ -77,7 +77,7 @@ def dist_env():
 
 
 def peaks():
-    """Roofline denominators: the machine's measured copy bandwidth and cuBLAS bf16 rate, else the fallback."""
+    """Roofline denominators: the measured copy bandwidth and cuBLAS bf16 rate (MEASURED_PEAKS.json), else the fallback."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())

@@ -1057,7 +1057,7 @@ bool launch_shapes_ok(const Plan* p, std::string* why) {
     const FwdShape f = fwd_shape(p, fwd_window(nc, p->Ex));
     const AdjShape a = adj_shape(p, adj_window(p->Nj_max, adj_kj(nc)));
     if (f.threads > 512 || a.threads > 512) {
-        *why = "launch shape exceeds 512 threads (too many points per pitch or elements for this build)";
+        *why = "launch shape exceeds 512 threads (too many points per pitch or elements for these kernels)";
         return false;
     }
     return true;

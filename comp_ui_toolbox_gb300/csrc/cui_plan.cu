@@ -338,7 +338,7 @@ cui_status select_device_and_shapes(Plan& p, int device) {
     while (nc < p.max_slots_per_f && nc < kMaxNC) nc = (nc < 8) ? nc * 2 : nc + 4;
     if (fwd_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin) ||
         adj_smem_bytes(&p, nc) + 1024 > static_cast<size_t>(smem_optin))
-        return set_error(CUI_ERR_UNSUPPORTED_SETUP, "grid line too long for the shared-memory staging of this build");
+        return set_error(CUI_ERR_UNSUPPORTED_SETUP, "grid line too long for the shared-memory staging of these kernels");
     std::string why;
     if (!launch_shapes_ok(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
     return CUI_OK;

@@ -109,9 +109,9 @@ __device__ __forceinline__ void fetch_band(uint32_t (&be)[kMaxBandPerThread], co
 }
 
 // chunk ch of variant v holds band entries ch..ch+3 (16 B at sA + (v*NCH + ch)*16).
-// A warp's 32 entries are written in 4 rounds; in round q lane l stores word
+// A warp's 32 entries are written in 4 passes; in pass q lane l stores word
 // l%4 of entry 8q + l/4 (taken from that lane by a shuffle), which puts the 32
-// stores of a round into 32 distinct banks.
+// stores of a pass into 32 distinct banks.
 __device__ __forceinline__ void store_chunks(unsigned char* sA, const uint32_t (&be)[kMaxBandPerThread], int NCH, int tid) {
     const int n = 2 * (NCH + 3);
     const int lane = tid & 31, wbase = tid - lane;

@@ -1,6 +1,6 @@
 """Generate the small golden fixtures of the Born operator from the FP64 oracle.
 
-The reference (MATLAB) cannot run here or on the GPU machine and its scripts pin
+The reference (MATLAB) cannot run without MATLAB and its scripts pin
 no numbers on this path, so these fixtures are oracle outputs: they freeze
 the restatement (tables, incident fields, forward and adjoint) so that any
 drift of the oracle is caught, and they give the CPU suite known answers.
