@@ -114,6 +114,9 @@ _SIGNATURES = {
     "cui_born_plan_create_setup_ex": (C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.c_int32, C.c_char_p,
                                                 C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]),
     "cui_born_plan_table_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "cui_born_autotune_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_int32)]),
+    "cui_born_set_launch_shapes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "cui_born_plan_destroy": (C.c_int, [C.c_void_p]),
     "cui_born_plan_info": (C.c_int, [C.c_void_p, C.POINTER(BornInfo)]),
     "cui_born_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -348,14 +351,23 @@ class OperatorBorn:
         self.precision = precision
 
     def autotune(self, n_objects: int = 1) -> dict:
-        """Keep the faster of the FP32 and split-BF16 paths for ``n_objects`` columns
-        (``cui_born_autotune``); returns the choice and both times."""
+        """Keep the faster of the FP32 and split-BF16 paths for ``n_objects`` columns and, on the
+        split-BF16 path, the fastest launch shapes (``cui_born_autotune``); returns the choice,
+        both times and the launch shapes (``cui_born_autotune_config``)."""
         import torch
         choice = C.c_int32(0)
         ms = (C.c_double * 2)()
         st = torch.cuda.current_stream().cuda_stream
         _check(self._lib.cui_born_autotune(self._plan, int(n_objects), C.byref(choice), ms, st))
-        return {"precision": "bf16x3" if choice.value == 1 else "fp32", "ms_fp32": ms[0], "ms_bf16x3": ms[1]}
+        tiles, fwd, adj = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        _check(self._lib.cui_born_autotune_config(self._plan, C.byref(tiles), C.byref(fwd), C.byref(adj)))
+        return {"precision": "bf16x3" if choice.value == 1 else "fp32", "ms_fp32": ms[0], "ms_bf16x3": ms[1],
+                "launch_shapes": {"narrow_tiles": tiles.value, "fwd_blocks": fwd.value or "rule",
+                                  "adj_blocks": adj.value or "rule"}}
+
+    def set_launch_shapes(self, narrow_tiles: int = 0, fwd_blocks: int = 0, adj_blocks: int = 0) -> None:
+        """Launch shapes of the split-BF16 line-unit kernels (``cui_born_set_launch_shapes``; 0: the rule)."""
+        _check(self._lib.cui_born_set_launch_shapes(self._plan, int(narrow_tiles), int(fwd_blocks), int(adj_blocks)))
 
     def device_status(self) -> int:
         """Read and clear the device status word (raises CuiError on a timed-out wait)."""

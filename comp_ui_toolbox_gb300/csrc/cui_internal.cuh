@@ -133,6 +133,12 @@ struct Plan {
     // line-unit tensor-core kernels (cui_tc2.cu; 2D, 4 grid points per pitch):
     // raw band rows [2][F][Nz][RowW] of packed bf16x2 (re, im), hi then lo
     int tc2 = 0;                     // 1 when the plan runs the line-unit kernels
+    // launch shapes picked by cui_born_autotune (0: the rule): column tiles of at most 32 columns
+    // instead of 64 (1), and the block counts the forward's line groups and the adjoint's frequency
+    // chunks aim at
+    int tune_tile = 0;
+    int tune_fwd_blocks = 0;
+    int tune_adj_blocks = 0;
     uint32_t* tr = nullptr;
     int64_t tr_vstride = 0;          // entries per variant
     int RowW = 0;                    // entries per row (lateral offsets rounded up to 4, zero padded)

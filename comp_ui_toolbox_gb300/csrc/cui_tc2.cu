@@ -1011,6 +1011,7 @@ Tile2 tile2(const Plan* p, int B) {
 // column tiles of both kernels: 64 columns (4 objects x up to 16 waves, N = 256 per MMA) when the
 // batch fills them, so that each staged table row feeds twice the columns; otherwise tile2
 Tile2 tile_fwd(const Plan* p, int B) {
+    if (p->tune_tile == 1) return tile2(p, B);  // the autotuner found the narrower tiles faster
     const int ms = std::max(1, p->max_slots_per_f);
     // (the adjoint's final gamma_hat of 2 lines x 4 column slots reuses its 16*64*Epad-byte V buffer)
     if (B >= 4 && ms >= 12 && ms <= 16 && p->Nx <= 16 * ((p->Ex + 15) / 16 * 16)) {
@@ -1035,7 +1036,8 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
     }
     const int n_lines = p->Nz;
     const size_t slab = static_cast<size_t>(p->S) * B * p->E * sizeof(float2);
-    int groups = std::max(1, std::min(n_lines, (8 * 152 + p->F * t.tiles - 1) / (p->F * t.tiles)));
+    const int target = p->tune_fwd_blocks > 0 ? p->tune_fwd_blocks : 8 * 152;  // blocks per launch
+    int groups = std::max(1, std::min(n_lines, (target + p->F * t.tiles - 1) / (p->F * t.tiles)));
     groups = static_cast<int>(std::max<size_t>(1, std::min<size_t>(groups, p->ws_part_bytes / std::max<size_t>(slab, 1))));
     const int lpg = (n_lines + groups - 1) / groups;
     groups = (n_lines + lpg - 1) / lpg;  // every group holds at least one line
@@ -1063,7 +1065,8 @@ cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nf
     const int Lz = (NT >= 64) ? AdjCfg<NT>::MAXL : 1;  // grid lines per block
     const int zblocks = (p->Nz + Lz - 1) / Lz;
     const size_t slab = static_cast<size_t>(B) * p->P * sizeof(float2);
-    int nfc = std::max(1, std::min(p->F, (8 * 152 + zblocks * t.tiles - 1) / (zblocks * t.tiles)));
+    const int target = p->tune_adj_blocks > 0 ? p->tune_adj_blocks : 8 * 152;  // blocks per launch
+    int nfc = std::max(1, std::min(p->F, (target + zblocks * t.tiles - 1) / (zblocks * t.tiles)));
     nfc = static_cast<int>(std::max<size_t>(1, std::min<size_t>(nfc, p->ws_part_bytes / std::max<size_t>(slab, 1))));
     const int fchunk = (p->F + nfc - 1) / nfc;
     nfc = (p->F + fchunk - 1) / fchunk;

@@ -1,5 +1,9 @@
 // Per-plan autotuner: times the contraction paths a plan can run for a given
-// object count and keeps the faster one.
+// object count and keeps the faster one; on the split-BF16 line-unit path it
+// then picks the launch shapes by a coordinate search over the column tiles
+// (64 columns or the narrower 16/32-column tiles) and the block counts the
+// forward's line groups and the adjoint's frequency chunks aim at, keeping
+// each candidate only when it lowers the timed forward + adjoint pair.
 //
 // Candidates: the FP32 CUDA-core kernels and the split-BF16 tensor-core
 // kernels (2D setups).  Both meet the operator's accuracy bound (relative L2
@@ -76,6 +80,7 @@ extern "C" cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, 
     }
     cudaMemsetAsync(g, 0, ng * sizeof(float2), st);
     const int32_t before = p.precision;
+    p.tune_tile = p.tune_fwd_blocks = p.tune_adj_blocks = 0;  // every search starts from the rule
     double t[2] = {-1.0, -1.0};
     cui_status s = cui_born_set_precision(plan, CUI_PRECISION_FP32);
     if (s == CUI_OK) s = time_path(&p, g, u, gh, n_objects, st, &t[0]);
@@ -85,19 +90,62 @@ extern "C" cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, 
         s = cui_born_set_precision(plan, CUI_PRECISION_BF16X3);
         if (s == CUI_OK) s = time_path(&p, g, u, gh, n_objects, st, &t[1]);
     }
+    const int32_t best = (t[1] >= 0.0 && t[1] < t[0]) ? CUI_PRECISION_BF16X3 : CUI_PRECISION_FP32;
+    if (s == CUI_OK) s = cui_born_set_precision(plan, best);
+    if (s == CUI_OK && best == CUI_PRECISION_BF16X3 && p.tc2) {
+        double t_best = t[1];
+        auto trial = [&](int* field, int value) -> cui_status {
+            const int old = *field;
+            *field = value;
+            double tv = 0.0;
+            const cui_status s2 = time_path(&p, g, u, gh, n_objects, st, &tv);
+            if (s2 == CUI_OK && tv < t_best)
+                t_best = tv;
+            else
+                *field = old;
+            return s2;
+        };
+        s = trial(&p.tune_tile, 1);
+        for (int v : {4 * 152, 16 * 152})
+            if (s == CUI_OK) s = trial(&p.tune_fwd_blocks, v);
+        for (int v : {4 * 152, 16 * 152})
+            if (s == CUI_OK) s = trial(&p.tune_adj_blocks, v);
+        if (s == CUI_OK) t[1] = t_best;
+    }
     cudaFree(g);
     cudaFree(gh);
     cudaFree(u);
     if (s != CUI_OK) {
         p.precision = before;
+        p.tune_tile = p.tune_fwd_blocks = p.tune_adj_blocks = 0;
         return s;
     }
-    const int32_t best = (t[1] >= 0.0 && t[1] < t[0]) ? CUI_PRECISION_BF16X3 : CUI_PRECISION_FP32;
-    if ((s = cui_born_set_precision(plan, best)) != CUI_OK) return s;
     if (precision) *precision = best;
     if (ms) {
         ms[0] = t[0];
         ms[1] = t[1];
     }
+    return CUI_OK;
+}
+
+extern "C" cui_status cui_born_autotune_config(const cui_born_plan* plan, int32_t* narrow_tiles, int32_t* fwd_blocks,
+                                               int32_t* adj_blocks) {
+    if (!plan) return cui::set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    const cui::Plan& p = plan->p;
+    if (narrow_tiles) *narrow_tiles = p.tune_tile;
+    if (fwd_blocks) *fwd_blocks = p.tune_fwd_blocks;
+    if (adj_blocks) *adj_blocks = p.tune_adj_blocks;
+    return CUI_OK;
+}
+
+extern "C" cui_status cui_born_set_launch_shapes(cui_born_plan* plan, int32_t narrow_tiles, int32_t fwd_blocks,
+                                                 int32_t adj_blocks) {
+    if (!plan) return cui::set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    if ((narrow_tiles != 0 && narrow_tiles != 1) || fwd_blocks < 0 || adj_blocks < 0)
+        return cui::set_error(CUI_ERR_INVALID_ARG, "narrow_tiles must be 0 or 1 and block counts >= 0");
+    cui::Plan& p = plan->p;
+    p.tune_tile = narrow_tiles;
+    p.tune_fwd_blocks = fwd_blocks;
+    p.tune_adj_blocks = adj_blocks;
     return CUI_OK;
 }

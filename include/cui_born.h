@@ -360,10 +360,25 @@ cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precision);
  * columns -- the FP32 CUDA-core kernels and, for 2D setups, the split-BF16
  * tensor-core kernels -- on `stream` and keeps the faster (as
  * cui_born_set_precision would).  Both paths meet the operator's accuracy bound.
+ * When the split-BF16 line-unit kernels win, it then searches their launch
+ * shapes (column tiles, blocks per launch; cui_born_autotune_config) one at a
+ * time and keeps each that lowers the timed pair; `ms[1]` is the tuned time.
  * Allocates and frees scratch buffers and synchronises: call it at set-up,
  * before any stream capture.  `precision` (may be NULL) receives the choice,
  * `ms` (may be NULL) the two times in ms (FP32, BF16X3; -1 when not run). */
 cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, int32_t* precision, double* ms, void* stream);
+/* Launch shapes the last cui_born_autotune picked for the split-BF16 line-unit
+ * kernels (0 everywhere: the built-in rule): `narrow_tiles` 1 when column tiles
+ * of at most 32 columns replaced the 64-column tiles, and the block counts the
+ * forward's line groups (`fwd_blocks`) and the adjoint's frequency chunks
+ * (`adj_blocks`) aim at.  Any pointer may be NULL. */
+cui_status cui_born_autotune_config(const cui_born_plan* plan, int32_t* narrow_tiles, int32_t* fwd_blocks,
+                                    int32_t* adj_blocks);
+/* Sets those launch shapes directly (0 everywhere restores the rule), e.g. to
+ * reuse a choice cui_born_autotune made on an earlier run.  Every combination
+ * gives results within the operator's accuracy bound. */
+cui_status cui_born_set_launch_shapes(cui_born_plan* plan, int32_t narrow_tiles, int32_t fwd_blocks,
+                                      int32_t adj_blocks);
 
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Device time of the two contraction kernels, from CUDA events recorded on

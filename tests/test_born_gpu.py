@@ -437,6 +437,43 @@ def test_bf16x3_wide_tiles_partial_tile_and_odd_lines(n_lines, n_obj):
     op.close()
 
 
+def test_bf16x3_launch_shapes_and_autotune():
+    """Every launch shape the autotuner can pick for the line-unit kernels (64- or 32-column tiles,
+    fewer or more blocks per launch) on a 64-column plan (16 waves, 6 objects, 17 grid lines), and
+    the shapes autotune keeps, against the FP32 path of the same plan; bound 1e-5 per object."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload("2d-batched")
+    w.f = w.f[:3]
+    w.n_points_axis = (w.n_points_axis[0], 17)
+    n_obj = 6
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
+    rng = np.random.default_rng(9)
+    g = rng.standard_normal((op.n_points, n_obj)) + 1j * rng.standard_normal((op.n_points, n_obj))
+    y = rng.standard_normal((op.n_observations, n_obj)) + 1j * rng.standard_normal((op.n_observations, n_obj))
+    u32 = op.forward(dev(g)).cpu().numpy()
+    a32 = op.adjoint(dev(y)).cpu().numpy()
+    op.set_precision("bf16x3")
+
+    def check():
+        u16 = op.forward(dev(g)).cpu().numpy()
+        a16 = op.adjoint(dev(y)).cpu().numpy()
+        assert op.device_status() == 0
+        for b in range(n_obj):
+            assert rel_l2(u16[:, b], u32[:, b]) <= TOL
+            assert rel_l2(a16[:, b], a32[:, b]) <= TOL
+
+    for shapes in [(0, 0, 0), (1, 0, 0), (0, 4 * 152, 4 * 152), (1, 16 * 152, 16 * 152), (0, 1, 1)]:
+        op.set_launch_shapes(*shapes)
+        check()
+    res = op.autotune(n_obj)
+    assert set(res["launch_shapes"]) == {"narrow_tiles", "fwd_blocks", "adj_blocks"}
+    if res["precision"] == "bf16x3":
+        check()
+    op.close()
+
+
 @pytest.mark.parametrize("name", CONFIGS)
 def test_energy_rx_matches_oracle(name):
     """Received energies ||Phi e_p||^2 (energy_rx_canonical, operator_born.m:718-859) against the
