@@ -82,3 +82,27 @@ def test_c_harness_builds_against_the_header(lib):
     """The plain C driver compiles as C99 against include/cui_born.h and links the library."""
     from comp_ui_toolbox_gb300 import build
     assert build.build_harness().exists()
+
+
+def test_table_storage_names_match_the_header_and_null_arguments(lib):
+    """The Python names of cui_table_storage carry the header's values; the storage query and the
+    launch-shape entry points reject NULL plans without a device call."""
+    from comp_ui_toolbox_gb300.born import _TABLE_STORAGE
+    text = HEADER.read_text()
+    values = {m.group(1): int(m.group(2)) for m in re.finditer(r"CUI_STORAGE_([A-Z]+)\s*=\s*(\d+)", text)}
+    assert {k.upper(): v for k, v in _TABLE_STORAGE.items()} == values
+    s = C.c_int32()
+    assert lib.cui_born_plan_table_storage(None, C.byref(s)) == 1
+    assert lib.cui_born_set_launch_shapes(None, 0, 0, 0) == 1
+    assert lib.cui_born_autotune_config(None, None, None, None) == 1
+    out = C.c_void_p()
+    assert lib.cui_born_plan_create_setup_ex(None, 1, 0, None, C.byref(out), None) == 1
+    assert out.value is None
+
+
+def test_unknown_table_storage_is_rejected_on_the_host():
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from oracle import configs
+    from tests.helpers import setup_kwargs
+    with pytest.raises(KeyError):
+        OperatorBorn.from_setup(**setup_kwargs(configs.small_config("c3")), table_storage="compressed")
