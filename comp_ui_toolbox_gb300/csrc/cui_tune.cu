@@ -106,9 +106,9 @@ extern "C" cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, 
             return s2;
         };
         s = trial(&p.tune_tile, 1);
-        for (int v : {4 * 152, 16 * 152})
+        for (int v : {4 * 152, 16 * 152, 32 * 152})
             if (s == CUI_OK) s = trial(&p.tune_fwd_blocks, v);
-        for (int v : {4 * 152, 16 * 152})
+        for (int v : {4 * 152, 16 * 152, 32 * 152})
             if (s == CUI_OK) s = trial(&p.tune_adj_blocks, v);
         if (s == CUI_OK) t[1] = t_best;
     }
