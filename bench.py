@@ -263,12 +263,37 @@ CPU_SAMPLE = {"2d-plain": (1, 8, None, None), "2d-gradient": (1, 8, None, None),
               "3d": (1, 1, None, 4)}
 
 
-def cpu_baseline(workload: str, n_objects: int):
+def cpu_baseline(workload: str, n_objects: int, op=None, w=None):
+    """Times the FP64 oracle on the workload's bounded sample.  With the device plan ``op`` of the
+    full workload ``w`` it also checks the plan's current path against the sample's FP64 outputs
+    (returned as ``check``): the forward rows of wave 0 at the sample's frequencies and receive
+    mixes, for the sample's seeded real Gaussian gamma (zero outside the sample's grid planes), and
+    the first column of the adjoint of exactly those rows."""
     from oracle.cpu_baseline import time_sample
     nw, nf, nm, npl = CPU_SAMPLE[workload]
-    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm, n_planes=npl)
-    return {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
-            "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
+    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm, n_planes=npl,
+                    check=op is not None)
+    out = {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
+           "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
+    check = None
+    if op is not None:
+        import numpy as np
+        import torch
+        c = r["check"]
+        F, Ps = len(w.f), c["P_sample"]
+        gam = np.zeros((op.n_points, n_objects), dtype=np.complex64)
+        gam[:Ps] = np.random.default_rng(c["seed"]).standard_normal((Ps, n_objects))
+        rows = np.array([m * F + fi for m in range(c["n_mix"]) for fi in c["f_idx"]])
+        u_dev = op.forward(torch.from_numpy(gam).cuda()).cpu().numpy().astype(np.complex128)[rows]
+        u_in = np.zeros((op.n_observations, n_objects), dtype=np.complex64)
+        u_in[rows] = c["u_rows"]
+        g_dev = op.adjoint(torch.from_numpy(u_in).cuda()).cpu().numpy().astype(np.complex128)[:Ps, 0]
+        rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
+        check = {"rel_l2_forward": rel(u_dev, c["u_rows"]), "rel_l2_adjoint": rel(g_dev, c["g0"]),
+                 "rows": int(len(rows)), "columns": int(n_objects),
+                 "what": "device path vs the FP64 oracle on the CPU sample: forward rows of wave 0 at the sample's "
+                         "frequencies and mixes (all columns), adjoint of those rows (first column)"}
+    return out, check
 
 
 TABLE_STORAGE = {
@@ -469,7 +494,9 @@ def run_ours(args):
         line["greedy"]["precision"] = args.precision
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline(args.workload, B)
+            # the check needs the full workload: the oracle's sample takes its frequencies from the full list
+            line["cpu_baseline"], check = cpu_baseline(args.workload, B, op if args.n_freq is None else None, w)
+            line["accuracy"] = dict(line["accuracy"] or {}, fp64_oracle_sample=check)
         except Exception as exc:  # report, never hide
             line["cpu_baseline"] = {"value": None, "error": repr(exc)}
     if rank == 0:

@@ -52,6 +52,7 @@ class BornConfig:
     n_objects: int = 1
     density: float = 0.02
     seed: int = 0
+    band: Optional[tuple] = None  # (f_min, f_max) of the excitation spectrum; None: the range of f
 
     @property
     def n_waves(self):
@@ -126,9 +127,11 @@ def small_config(name: str) -> BornConfig:
 
 
 # --------------------------------------------------------------------------
-def excitation_spectrum(f: np.ndarray) -> np.ndarray:
-    """Smooth synthetic excitation x impulse-response spectrum (Gaussian in f)."""
-    fc = 0.5 * (f.min() + f.max())
+def excitation_spectrum(f: np.ndarray, band=None) -> np.ndarray:
+    """Smooth synthetic excitation x impulse-response spectrum (Gaussian in f, centred on the band:
+    the range of ``f`` unless ``band`` = (f_min, f_max) is given)."""
+    lo, hi = (f.min(), f.max()) if band is None else band
+    fc = 0.5 * (lo + hi)
     return np.exp(-0.5 * ((f - fc) / (0.4 * fc)) ** 2)
 
 
@@ -148,7 +151,7 @@ def wave_vd(cfg: BornConfig, wave: Wave, f: np.ndarray) -> np.ndarray:
     else:
         raise ValueError(wave.kind)
     tau = quantize_delays(tau)
-    return excitation_spectrum(f)[:, None] * apod[None, :] * np.exp(-2j * np.pi * f[:, None] * tau[None, :])
+    return excitation_spectrum(f, cfg.band)[:, None] * apod[None, :] * np.exp(-2j * np.pi * f[:, None] * tau[None, :])
 
 
 def mix_weights(cfg: BornConfig):

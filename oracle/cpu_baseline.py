@@ -35,6 +35,7 @@ def _sample_config(name: str, n_waves: int, n_freq: int, n_planes=None):
     from oracle import configs
     cfg = configs.config(name)
     f_idx = np.linspace(0, len(cfg.f) - 1, n_freq).round().astype(int)
+    cfg.band = (float(cfg.f.min()), float(cfg.f.max()))  # the full workload's excitation spectrum
     cfg.f = cfg.f[f_idx]
     cfg.waves = cfg.waves[:n_waves]
     if n_planes is not None:
@@ -56,25 +57,34 @@ def _init(name, n_waves, n_freq, seed, n_objects=1, n_planes=None):
 
 
 def _work(args):
-    """Forward and adjoint restricted to a chunk of mixes of every measurement."""
+    """Forward and adjoint restricted to a chunk of mixes of every measurement.  With ``want``
+    the chunk's forward rows and the first column of its adjoint come back too (for checking a
+    device result against them; they are computed inside the timed region anyway)."""
     import dataclasses
     from oracle import adjoint_quick_cpu, forward_quick_cpu
-    lo, hi = args
+    lo, hi = args[0], args[1]
+    want = len(args) > 2 and args[2]
     if hi <= lo:  # warm-up call: the initializer has built the tables
-        return 0.0, 0.0
+        return 0.0, 0.0, None, None
     b = _STATE["b"]
     meas = [dataclasses.replace(m, mixes=m.mixes[lo:hi]) for m in b.op.measurements]
     op = dataclasses.replace(b.op, measurements=meas)
     t0 = time.perf_counter()
     u = forward_quick_cpu(op, _STATE["gamma"])
     g = adjoint_quick_cpu(op, u)
-    return time.perf_counter() - t0, float(np.abs(g).sum())
+    t = time.perf_counter() - t0
+    return t, float(np.abs(g).sum()), (u if want else None), (g[:, 0].copy() if want else None)
 
 
 def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: int | None = None,
                 repeats: int = 1, seed: int = 0, n_objects: int = 1, n_mixes: int | None = None,
-                n_planes: int | None = None):
+                n_planes: int | None = None, check: bool = False):
     """Seconds per forward+adjoint apply of the full workload, extrapolated from a sample.
+
+    With ``check`` the result also holds the sample's FP64 outputs (``"check"``): the forward rows
+    of wave 0 (mix-major, then the sample frequencies ``f_idx`` of the full workload), the first
+    column of the adjoint of those rows, the seed of the real Gaussian gamma (P_sample x
+    n_objects) and the sizes, for comparing a device apply of the full workload with them.
 
     ``n_mixes`` keeps only the first receive mixes of every wave (work is linear
     in the mixes when every mix has the same active elements, as in the
@@ -101,12 +111,16 @@ def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: 
     with ctx.Pool(procs, initializer=_init, initargs=(name, n_waves, n_freq, seed, n_objects, n_planes)) as pool:
         pool.map(_work, [(0, 0)] * procs)  # wait until every worker holds its tables
         times = []
-        for _ in range(repeats):
+        outs = None
+        for r in range(repeats):
             # critical path of the parallel apply: the slowest worker's own compute time
-            times.append(max(t for t, _ in pool.map(_work, chunks, chunksize=1)))
+            res = pool.map(_work, [(lo, hi, check and r == 0) for lo, hi in chunks], chunksize=1)
+            times.append(max(t for t, _, _, _ in res))
+            if check and r == 0:
+                outs = res
     t_sample = min(times)
     t_full = t_sample * (S_full / S_sample) * (n_mix_full / n_mix) * (P_full / P_sample)
-    return {
+    result = {
         "seconds_sample": t_sample,
         "seconds_full_apply": t_full,
         "applies_per_s": n_objects / t_full,  # object-applies: all columns go through one BLAS call per element
@@ -121,6 +135,12 @@ def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: 
                   f"sample rate x {S_sample}/{S_full} x {n_mix}/{n_mix_full}"
                   + (f" x {P_sample}/{P_full}" if P_sample != P_full else ""),
     }
+    if check:
+        f_idx = np.linspace(0, len(full.f) - 1, n_freq).round().astype(int)
+        result["check"] = {"u_rows": np.concatenate([o[2] for o in outs], axis=0),
+                           "g0": np.sum([o[3] for o in outs], axis=0), "f_idx": [int(i) for i in f_idx],
+                           "n_mix": n_mix, "P_sample": P_sample, "seed": seed}
+    return result
 
 
 if __name__ == "__main__":
