@@ -96,7 +96,8 @@ class BornTiming(C.Structure):
 
 class BornInfo(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("n_points", "n_observations", "n_elements", "n_slots", "n_f_unique",
-                                         "table_bytes", "incident_bytes", "workspace_bytes", "contraction_macs")]
+                                         "table_bytes", "incident_bytes", "workspace_bytes", "contraction_macs",
+                                         "channel_macs", "folded_bytes", "folded_sums", "device_allocations")]
 
 
 _lib = None
@@ -133,6 +134,10 @@ _SIGNATURES = {
     "cui_born_vjp_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                     C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
     "cui_born_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "cui_born_host_path": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "cui_born_lasso_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
+                                      C.c_void_p, C.c_float, C.c_int32]),
+    "cui_born_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64]),
     "cui_born_energy_rx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "cui_born_omp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int64), C.c_void_p,
                                C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_void_p]),
@@ -345,9 +350,13 @@ class OperatorBorn:
     def __exit__(self, *exc):
         self.close()
 
+    PRECISIONS = {"fp32": 0, "bf16x3": 1, "bf16x3-folded": 2}
+
     def set_precision(self, precision: str) -> None:
-        """``"fp32"`` (CUDA cores) or ``"bf16x3"`` (split-BF16 tcgen05 tensor cores)."""
-        _check(self._lib.cui_born_set_precision(self._plan, {"fp32": 0, "bf16x3": 1}[precision]))
+        """``"fp32"`` (CUDA cores), ``"bf16x3"`` (split-BF16 tcgen05 tensor cores over slots and
+        elements) or ``"bf16x3-folded"`` (split-BF16 tcgen05 GEMMs against the operator folded over
+        its receive mixes and stored in device memory, built on the first switch)."""
+        _check(self._lib.cui_born_set_precision(self._plan, self.PRECISIONS[precision]))
         self.precision = precision
 
     def autotune(self, n_objects: int = 1) -> dict:
@@ -368,6 +377,25 @@ class OperatorBorn:
     def set_launch_shapes(self, narrow_tiles: int = 0, fwd_blocks: int = 0, adj_blocks: int = 0) -> None:
         """Launch shapes of the split-BF16 line-unit kernels (``cui_born_set_launch_shapes``; 0: the rule)."""
         _check(self._lib.cui_born_set_launch_shapes(self._plan, int(narrow_tiles), int(fwd_blocks), int(adj_blocks)))
+
+    def refresh_info(self) -> dict:
+        """Re-read the plan's work and storage figures (``cui_born_plan_info``), for instance after
+        switching to the folded operator, which adds its matrix."""
+        info = BornInfo()
+        _check(self._lib.cui_born_plan_info(self._plan, C.byref(info)))
+        self.info = {n: int(getattr(info, n)) for n, _ in BornInfo._fields_}
+        return self.info
+
+    def host_path(self) -> str:
+        """``"direct"`` when the host entry points' kernels read and write the caller's arrays through
+        the host page tables, ``"staging"`` when the data pass through pinned buffers."""
+        d = C.c_int32()
+        _check(self._lib.cui_born_host_path(self._plan, C.byref(d)))
+        return "direct" if d.value else "staging"
+
+    def set_wait_limit(self, nanoseconds: int = 0) -> None:
+        """Wall-clock limit of the tensor-core kernels' waits (``cui_born_set_wait_limit``; 0: 1 s)."""
+        _check(self._lib.cui_born_set_wait_limit(self._plan, int(nanoseconds)))
 
     def device_status(self) -> int:
         """Read and clear the device status word (raises CuiError on a timed-out wait)."""

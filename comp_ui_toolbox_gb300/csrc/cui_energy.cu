@@ -145,7 +145,8 @@ extern "C" cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, voi
     Plan& p = plan->p;
     if (p.Nx > kEnergyThreads * kEnergyMaxPX)
         return set_error(CUI_ERR_UNSUPPORTED_SETUP, "energy_rx covers lateral grid lines of up to 1024 points");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     const int lines = p.Ny * p.Nz;
     const int64_t cap = static_cast<int64_t>(p.ws_part_bytes / (sizeof(float) * static_cast<size_t>(p.P)));

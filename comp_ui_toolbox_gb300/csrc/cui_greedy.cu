@@ -416,7 +416,8 @@ extern "C" cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, 
     const int64_t n = p.n_obs, P = p.P;
     const int kmax = static_cast<int>(std::min<int64_t>(n_atoms_max, n));
     if (kmax < 1) return set_error(CUI_ERR_INVALID_ARG, "n_atoms_max must be >= 1");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // scratch for the whole solve, allocated per call (OMP is a host-driven loop with a
@@ -563,7 +564,8 @@ extern "C" cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* 
         return set_error(CUI_ERR_INVALID_ARG, "3 * sparsity exceeds the observations (under-determined least squares)");
     const int iters = static_cast<int>(std::min<int64_t>(n_iter_max, n));
     if (iters < 1) return set_error(CUI_ERR_INVALID_ARG, "n_iter_max must be >= 1");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 

@@ -160,7 +160,8 @@ cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_c
     if (!input || !output || n_objects < 1 || n_objects > p.max_objects || ld_in < rows_in || ld_out < rows_out)
         return set_error(CUI_ERR_INVALID_ARG, "input must be a matrix with the operator's number of rows "
                                               "(combined_quick_gpu:NoValidDoubleMatrix)");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     if (host_direct(p)) {
         cui_status s = ensure_device_stage(p);
@@ -202,7 +203,8 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
     if (!gamma || !u_meas || !grad || n_objects < 1 || n_objects > p.max_objects || ld_gamma < p.P ||
         ld_u < p.n_obs || ld_grad < p.P)
         return set_error(CUI_ERR_INVALID_ARG, "invalid arguments to cui_born_vjp_host");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     if (host_direct(p)) {
         cui_status s = ensure_device_stage(p);
@@ -250,3 +252,61 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
 }
 
 }  // extern "C"
+
+extern "C" cui_status cui_born_lasso_host(cui_born_plan* plan, const cui_complex64* u_meas, int64_t ld_u,
+                                          int32_t n_objects, cui_complex64* gamma, int64_t ld_gamma,
+                                          const float* lambda, float step, int32_t n_iter) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    Plan& p = plan->p;
+    if (!u_meas || !gamma || !lambda || n_objects < 1 || n_objects > p.max_objects || ld_u < p.n_obs ||
+        ld_gamma < p.P || n_iter < 0 || !(step > 0.f))
+        return set_error(CUI_ERR_INVALID_ARG, "invalid arguments to cui_born_lasso_host");
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
+    if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
+    const bool direct = host_direct(p);
+    cui_status s = direct ? ensure_device_stage(p) : ensure_stage(p);
+    if (s != CUI_OK) return s;
+    const size_t ng = static_cast<size_t>(p.P) * n_objects, nu = static_cast<size_t>(p.n_obs) * n_objects;
+    // thresholds in the loss slot of the device staging (one float per object)
+    if ((e = cudaMemcpyAsync(p.d_stage_loss, lambda, sizeof(float) * n_objects, cudaMemcpyHostToDevice, 0)) !=
+        cudaSuccess)
+        return check_cuda(e, "upload lambda");
+    if (direct) {
+        host_in_kernel<<<host_grid(p.n_obs, n_objects), 256>>>(u_meas, ld_u, p.n_obs, p.d_stage_aux);
+        host_in_kernel<<<host_grid(p.P, n_objects), 256>>>(gamma, ld_gamma, p.P, p.d_stage_in);
+        count_launch(2);
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
+    } else {
+        pack(u_meas, ld_u, p.n_obs, n_objects, p.h_stage_aux);
+        pack(gamma, ld_gamma, p.P, n_objects, p.h_stage_in);
+        if ((e = cudaMemcpyAsync(p.d_stage_aux, p.h_stage_aux, sizeof(float2) * nu, cudaMemcpyHostToDevice, 0)) !=
+                cudaSuccess ||
+            (e = cudaMemcpyAsync(p.d_stage_in, p.h_stage_in, sizeof(float2) * ng, cudaMemcpyHostToDevice, 0)) !=
+                cudaSuccess)
+            return check_cuda(e, "upload");
+    }
+    s = lasso_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, step, p.d_stage_loss, n_iter, nullptr, 0);
+    if (s != CUI_OK) return s;
+    if (direct) {
+        host_out_kernel<<<host_grid(p.P, n_objects), 256>>>(p.d_stage_in, p.P, gamma, ld_gamma);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host output");
+        return check_cuda(cudaStreamSynchronize(0), "synchronize");
+    }
+    if ((e = cudaMemcpyAsync(p.h_stage_out, p.d_stage_in, sizeof(float2) * ng, cudaMemcpyDeviceToHost, 0)) != cudaSuccess)
+        return check_cuda(e, "download");
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return check_cuda(e, "synchronize");
+    unpack(p.h_stage_out, p.P, n_objects, gamma, ld_gamma);
+    return CUI_OK;
+}
+
+extern "C" cui_status cui_born_host_path(cui_born_plan* plan, int32_t* direct) {
+    using namespace cui;
+    if (!plan || !direct) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
+    const DeviceGuard dev_guard(plan->p.device);
+    if (dev_guard.err != cudaSuccess) return check_cuda(dev_guard.err, "cudaSetDevice");
+    *direct = host_direct(plan->p) ? 1 : 0;
+    return CUI_OK;
+}

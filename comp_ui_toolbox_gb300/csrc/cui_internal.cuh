@@ -106,6 +106,7 @@ struct Plan {
     int Nj_max = 1;                 // steps per residue along x
     int Ni = 1;                     // staged table entries per residue
     size_t table_bytes = 0, incident_bytes = 0, workspace_bytes = 0;
+    int64_t channel_entries = 0;     // sum over slots of min(rows, distinct active elements) x points
 
     // host-side pinned staging for the FP64 host entry points
     float2* h_stage_in = nullptr;
@@ -122,7 +123,8 @@ struct Plan {
     std::vector<int> h_f_slot_ptr, h_f_slot_list, h_slot_f;
     HostMeta h_meta;                 // emptied once uploaded
 
-    // split-BF16 tensor-core path (cui_tc.cu): 0 = FP32 CUDA cores, 1 = BF16x3 tensor cores
+    // contraction path: 0 = FP32 CUDA cores, 1 = split-BF16 tensor cores over (slot, element)
+    // (cui_tc.cu, cui_tc2.cu), 2 = split-BF16 GEMMs against the folded operator (cui_phi.cu)
     int precision = 0;
     uint32_t* tb = nullptr;          // band arrays [4][F][Nz][Noy][ppx][Nb] of packed bf16x2
     int64_t tb_vstride = 0;
@@ -153,6 +155,22 @@ struct Plan {
     float2* ws_galign = nullptr;     // [max_objects][P] aligned copy of a misaligned gamma (forward)
     uint32_t* ws_vs = nullptr;       // split-BF16 V tiles of the adjoint [F][tiles][tile bytes / 4]
     int* ws_status = nullptr;        // device status word (bounded waits that gave up)
+    // wall-clock limit of every bounded wait of the tensor-core kernels (a wait that runs out
+    // raises the status word); the waits that drain in-flight copies keep a fixed 1 s
+    uint64_t wait_limit_ns = 1000000000ull;
+
+    // folded operator (cui_phi.cu, precision 2): observation x point matrix in split bf16,
+    // 16-byte pieces per (row, 8-point block, component, half), rows padded to 256 and points
+    // to 256; B forms of one 64-object pass of gamma and of u; chunk partial sums
+    uint8_t* phi = nullptr;
+    size_t phi_bytes = 0;
+    int64_t phi_rows_pad = 0;
+    int64_t phi_npb = 0;             // 8-point blocks
+    int64_t phi_reps = 0;            // distinct element sums the build formed
+    int phi_fwd_kc = 1, phi_adj_kc = 1;
+    uint8_t* phi_gforms = nullptr;
+    uint8_t* phi_uforms = nullptr;
+    float2* phi_part = nullptr;
 
     // per-kernel timing (diagnostics): event pairs around contraction launches
     bool timing = false;
@@ -161,6 +179,25 @@ struct Plan {
     size_t ev_used = 0;
 
     std::vector<void*> allocations;  // every device allocation (freed on destroy)
+    int n_device_allocs = 0;         // device allocations attempted so far (fault injection counts them)
+};
+
+// Makes a device current for the scope of an entry point and restores the caller's current device
+// on return, so that calling the library never changes which device the caller's own CUDA calls use.
+// DeviceGuard(-1) only restores (plan creation selects the device itself once it is validated).
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (device >= 0 && device != prev) err = cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
 };
 
 // error state (thread-local message) ------------------------------------
@@ -177,6 +214,8 @@ cui_status build_metadata(Plan& p, const std::vector<MeasIn>& ms, const std::vec
 cui_status select_device_and_shapes(Plan& p, int device);
 cui_status upload_metadata_and_workspace(Plan& p);
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes);
+// fault injection of device allocations (CUI_BORN_FAIL_ALLOC=N: the plan's N-th allocation fails)
+bool injected_alloc_failure(Plan& p);
 // table cache (cui_cache.cu): canonical key of the setup fields the device tables depend on,
 // its file path under `dir` (the incident fields alone when the table is not stored), and
 // loading / storing p.table (when stored) and p.p_in
@@ -215,6 +254,13 @@ bool tc2_supported(const Plan* p, std::string* why);
 cui_status tc2_prepare(Plan& p);
 cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* groups);
 cudaError_t launch_adj_tc2(Plan* p, int B, cudaStream_t st, int* nfc);
+
+// folded operator (split-BF16 GEMMs against the stored observation x point matrix)
+size_t phi_matrix_bytes(const Plan* p);
+bool phi_supported(const Plan* p, std::string* why);
+cui_status phi_prepare(Plan& p);
+cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* n_kc);
+cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc);
 
 // timing hooks around a contraction launch (no-ops unless timing is enabled)
 cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st);

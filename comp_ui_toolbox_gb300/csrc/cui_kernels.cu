@@ -947,8 +947,24 @@ int grid_1d(int64_t n, int threads) {
     return static_cast<int>(std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32));
 }
 
+// forward against the folded operator: 64-object GEMM passes, each reduced over its K chunks into u
+cudaError_t run_forward_phi(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
+    for (int b0 = 0; b0 < B; b0 += 64) {
+        const int nb = std::min(64, B - b0);
+        int nkc = 1;
+        cudaError_t e = launch_fwd_phi(p, gamma + static_cast<int64_t>(b0) * ldg, ldg, nb, st, &nkc);
+        if (e != cudaSuccess) return e;
+        reduce_fchunks_kernel<<<grid_1d(static_cast<int64_t>(nb) * p->n_obs, 256), 256, 0, st>>>(
+            p->phi_part, nkc, nb, p->n_obs, u + static_cast<int64_t>(b0) * ldu, ldu);
+        count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
     cudaError_t e;
+    if (p->precision == 2) return run_forward_phi(p, gamma, ldg, B, u, ldu, st);
     int groups = p->fwd_groups;
     if (p->precision == 1 && p->tc2) {
         e = launch_fwd_tc2(p, gamma, ldg, B, st, &groups);
@@ -995,20 +1011,40 @@ struct IstaArgs {
     const float* lambda;  // [B] device
 };
 
-// final reduction of the adjoint's frequency-chunk partials: plain sum into g, or the ISTA update of g
-cudaError_t finish_adjoint(Plan* p, int nfc, int B, float2* g, int64_t ldg, const IstaArgs* ista, cudaStream_t st) {
+// final reduction of the adjoint's chunk partials part[nfc][B][P]: plain sum into g, or the ISTA update of g
+cudaError_t finish_adjoint(Plan* p, const float2* part, int nfc, int B, float2* g, int64_t ldg, const IstaArgs* ista,
+                           cudaStream_t st) {
     const int64_t m = static_cast<int64_t>(B) * p->P;
     if (ista)
-        ista_reduce_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg, ista->step, ista->lambda);
+        ista_reduce_kernel<<<grid_1d(m, 256), 256, 0, st>>>(part, nfc, B, p->P, g, ldg, ista->step, ista->lambda);
     else
-        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(p->ws_part, nfc, B, p->P, g, ldg);
+        reduce_fchunks_kernel<<<grid_1d(m, 256), 256, 0, st>>>(part, nfc, B, p->P, g, ldg);
     count_launch();
     return cudaGetLastError();
+}
+
+// adjoint against the folded operator: 64-object GEMM passes straight from the observations
+// (no unmixing: the mixes are inside the matrix)
+cudaError_t run_adjoint_phi(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
+                            const IstaArgs* ista) {
+    for (int b0 = 0; b0 < B; b0 += 64) {
+        const int nb = std::min(64, B - b0);
+        int nkc = 1;
+        cudaError_t e = launch_adj_phi(p, u + static_cast<int64_t>(b0) * ldu, ldu, nb, st, &nkc);
+        if (e != cudaSuccess) return e;
+        IstaArgs is{};
+        if (ista) is = IstaArgs{ista->step, ista->lambda + b0};
+        if ((e = finish_adjoint(p, p->phi_part, nkc, nb, g + static_cast<int64_t>(b0) * ldg, ldg, ista ? &is : nullptr,
+                                st)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
                         const IstaArgs* ista = nullptr) {
     cudaError_t e;
+    if (p->precision == 2) return run_adjoint_phi(p, u, ldu, B, g, ldg, st, ista);
     if (use_mix_tile(p, B)) {
         MixTileArgs t = mix_tile_args(p, B);
         t.uin = u; t.ldu = ldu; t.V = p->ws_G;
@@ -1035,7 +1071,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         } else if ((e = launch_adj_tc(p, B, st)) != cudaSuccess) {
             return e;
         }
-        return finish_adjoint(p, nfc, B, g, ldg, ista, st);
+        return finish_adjoint(p, p->ws_part, nfc, B, g, ldg, ista, st);
     }
     switch (pick_nc(p->max_slots_per_f)) {
         case 1: e = launch_adj<1>(p, B, st); break;
@@ -1047,7 +1083,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         default: e = launch_adj<16>(p, B, st); break;
     }
     if (e != cudaSuccess) return e;
-    return finish_adjoint(p, p->adj_nfc, B, g, ldg, ista, st);
+    return finish_adjoint(p, p->ws_part, p->adj_nfc, B, g, ldg, ista, st);
 }
 
 }  // namespace
@@ -1150,15 +1186,15 @@ size_t loss_workspace_floats(int max_objects) { return static_cast<size_t>(kLoss
 // ---------------------------------------------------------------------------
 // Forward apply that allocates nothing.
 //
-// Some callers cannot call cudaMalloc when they apply the operator: code that
-// runs while a CUDA graph is being captured on the stream (an allocation
-// cannot be captured), hosts that hand their plug-ins a fixed memory budget
-// and forbid further device allocations, and real-time loops that must not
-// touch the allocator between frames.  cui_born_forward_static serves them:
-// it reads the plan's tables like cui_born_forward but keeps its partial sums
-// in a fixed file-scope device array instead of the plan's workspace, and it
-// never allocates.  The array is kStaticScratchBytes large and is held by
-// every GPU that loads the library until the process exits.
+// Some callers cannot call cudaMalloc when they apply the operator: hosts
+// that hand their plug-ins a fixed device-memory budget and forbid further
+// allocations, and real-time loops that must not enter the allocator (which
+// may synchronise the device) between frames.  cui_born_forward_static serves
+// them: it reads the plan's tables like cui_born_forward but keeps its partial
+// sums in a fixed file-scope device array instead of the plan's workspace, and
+// it never allocates.  It runs the FP32 CUDA-core kernels whatever the plan's
+// precision.  The array is kStaticScratchBytes large and is held by every GPU
+// that loads the library until the process exits.
 // ---------------------------------------------------------------------------
 namespace cui {
 namespace {
@@ -1174,7 +1210,7 @@ float2* g_static_ptr[kMaxDevices] = {};
 // array is only a host-side stand-in; kernels need this address.  Looked up
 // once per device, on the first call on that device.
 cudaError_t static_scratch(int device, float2** out) {
-    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;  // rejected by the caller first
     std::lock_guard<std::mutex> lock(g_static_mu);
     if (!g_static_ptr[device]) {
         void* p = nullptr;
@@ -1186,10 +1222,9 @@ cudaError_t static_scratch(int device, float2** out) {
     return cudaSuccess;
 }
 
-template <int NC>
-cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, int B, float2* part, int groups,
-                              int lines_per_group, cudaStream_t st) {
-    constexpr int KE = fwd_ke(NC);
+template <int NC, int KE>
+cudaError_t launch_fwd_static_k(const Plan* p, const float2* gamma, int64_t ldg, int B, float2* part, int groups,
+                                int lines_per_group, cudaStream_t st) {
     const FwdShape sh = fwd_shape(p, KE);
     FwdArgs a;
     a.g = geom_of(p);
@@ -1204,14 +1239,25 @@ cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, i
     const size_t smem = fwd_smem_bytes(p, NC);
     // a table that is not stored (generated or streamed) is generated inside the kernel here: the
     // chunk buffer of a streamed plan may be in use by work on another stream
-    void (*kern)(const FwdArgs) = p->table_mode != CUI_STORAGE_STORED ? fwd_gen_kernel<NC, KE>
-                                                                    : fwd_dense_kernel<NC, KE>;
+    // the body cui_born_forward launches for this plan (register-capped for 3D plans and wide shapes)
+    void (*kern)(const FwdArgs) = p->table_mode != CUI_STORAGE_STORED      ? fwd_gen_kernel<NC, KE>
+                                  : p->n_dims == 3 || NC * KE >= 16         ? fwd_dense3_kernel<NC, KE>
+                                                                            : fwd_dense_kernel<NC, KE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     dim3 grid(groups * a.n_eyb, p->F, B * a.npass);
     kern<<<grid, sh.threads, smem, st>>>(a);
     count_launch();
     return cudaGetLastError();
+}
+
+// the register window cui_born_forward picks (fwd_window)
+template <int NC>
+cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, int B, float2* part, int groups,
+                              int lines_per_group, cudaStream_t st) {
+    if (fwd_window(NC, p->Ex) == 2)
+        return launch_fwd_static_k<NC, 2>(p, gamma, ldg, B, part, groups, lines_per_group, st);
+    return launch_fwd_static_k<NC, fwd_ke(NC)>(p, gamma, ldg, B, part, groups, lines_per_group, st);
 }
 
 }  // namespace
@@ -1230,12 +1276,22 @@ extern "C" cui_status cui_born_forward_static(cui_born_plan* plan, const cui_com
         return set_error(CUI_ERR_INVALID_ARG,
                          "cui_born_forward_static: slots x objects x elements x 16 B exceeds the 16 MiB static "
                          "scratch; use cui_born_forward or fewer objects per call");
+    if (p->device < 0 || p->device >= kMaxDevices)
+        return set_error(CUI_ERR_INVALID_ARG, "cui_born_forward_static: device index " + std::to_string(p->device) +
+                                                  " beyond the " + std::to_string(kMaxDevices) +
+                                                  " devices its scratch address table covers");
+    // one grid z index per (object, pass over the frequency's slots): the launch limit is 65535
+    const int64_t npass = (p->max_slots_per_f + pick_nc(p->max_slots_per_f) - 1) / pick_nc(p->max_slots_per_f);
+    if (static_cast<int64_t>(n_objects) * npass > 65535)
+        return set_error(CUI_ERR_INVALID_ARG, "cui_born_forward_static: objects x slot passes exceeds 65535 (the "
+                                              "launch's z extent); use cui_born_forward or fewer objects per call");
     const int n_lines = p->Ny * p->Nz;
     int groups = static_cast<int>(std::min<size_t>(kStaticScratchBytes / slab - 1, static_cast<size_t>(p->fwd_groups)));
     groups = std::max(1, std::min(groups, n_lines));
     const int lines_per_group = (n_lines + groups - 1) / groups;
     groups = (n_lines + lines_per_group - 1) / lines_per_group;
-    cudaError_t e = cudaSetDevice(p->device);
+    const DeviceGuard dev_guard(p->device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     float2* scratch = nullptr;
     if ((e = static_scratch(p->device, &scratch)) != cudaSuccess) return check_cuda(e, "cudaGetSymbolAddress");

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -41,10 +42,20 @@ cui_status check_cuda(cudaError_t e, const char* what) {
 
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Fault injection for the cleanup paths (tests): with CUI_BORN_FAIL_ALLOC=N in the environment, the
+// N-th device allocation of each plan (counted over its whole life: creation, precision switches)
+// fails as an out-of-memory error would, before cudaMalloc is called.
+bool injected_alloc_failure(Plan& p) {
+    const char* env = std::getenv("CUI_BORN_FAIL_ALLOC");
+    ++p.n_device_allocs;
+    return env && env[0] && std::atoi(env) == p.n_device_allocs;
+}
+
 namespace {
 
 template <typename T>
 cudaError_t dalloc(Plan& p, T** ptr, size_t n) {
+    if (injected_alloc_failure(p)) return cudaErrorMemoryAllocation;
     void* v = nullptr;
     cudaError_t e = cudaMalloc(&v, std::max<size_t>(n, 1) * sizeof(T));
     if (e == cudaSuccess) {
@@ -449,6 +460,25 @@ cui_status upload_metadata_and_workspace(Plan& p) {
         CUI_TRY(upload(p, &p.egroup_ptr, gptr));
         CUI_TRY(upload(p, &p.egroup_slots, gslots));
     }
+    {
+        // channel-contraction entries per object (dense gamma): per slot, the rows it feeds or the
+        // distinct elements they read, whichever is fewer, times the grid points
+        int64_t ch = 0;
+        std::vector<int> seen(p.E, -1);
+        for (int s = 0; s < p.S; ++s) {
+            int n_el = 0;
+            const int r0 = h.slot_row_ptr[s], r1 = h.slot_row_ptr[s + 1];
+            for (int i = r0; i < r1; ++i) {
+                const int m = h.row_mix[h.slot_rows[i]];
+                for (int a = 0; a < h.mix_nact[m]; ++a) {
+                    const int e = h.act[h.mix_act_off[m] + a];
+                    if (seen[e] != s) { seen[e] = s; ++n_el; }
+                }
+            }
+            ch += std::min(r1 - r0, n_el);
+        }
+        p.channel_entries = ch * p.P;
+    }
     p.h_meta = HostMeta();
 
     const int B = p.max_objects;
@@ -466,6 +496,9 @@ cui_status upload_metadata_and_workspace(Plan& p) {
 }
 
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes) {
+    if (injected_alloc_failure(p))
+        return set_error(CUI_ERR_OOM, "cudaMalloc: injected allocation failure " + std::to_string(p.n_device_allocs) +
+                                          " (CUI_BORN_FAIL_ALLOC)");
     void* v = nullptr;
     cudaError_t e = cudaMalloc(&v, std::max<size_t>(bytes, 1));
     if (e != cudaSuccess) return check_cuda(e, "cudaMalloc");
@@ -540,6 +573,7 @@ cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, 
     *plan = nullptr;
     cui_born_plan* h = new (std::nothrow) cui_born_plan();
     if (!h) return set_error(CUI_ERR_OOM, "host allocation failed");
+    const cui::DeviceGuard restore(-1);  // creation makes the plan's device current; the caller's is restored
     cui_status s;
     try {
         s = cui::create(desc, max_objects, h->p);
@@ -557,7 +591,7 @@ cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, 
 
 cui_status cui_born_plan_destroy(cui_born_plan* plan) {
     if (!plan) return CUI_OK;
-    cudaSetDevice(plan->p.device);
+    const cui::DeviceGuard dev_guard(plan->p.device);
     cui::free_plan(plan->p);
     delete plan;
     return CUI_OK;
@@ -575,6 +609,10 @@ cui_status cui_born_plan_info(const cui_born_plan* plan, cui_born_info* info) {
     info->incident_bytes = static_cast<int64_t>(p.incident_bytes);
     info->workspace_bytes = static_cast<int64_t>(p.workspace_bytes);
     info->contraction_macs = static_cast<int64_t>(p.S) * p.E * p.P;
+    info->channel_macs = p.channel_entries;
+    info->folded_bytes = static_cast<int64_t>(p.phi_bytes);
+    info->folded_sums = p.phi_reps;
+    info->device_allocations = p.n_device_allocs;
     return CUI_OK;
 }
 
@@ -590,7 +628,7 @@ cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int
     cui_status s = cui::check_apply(plan, gamma, ld_gamma, plan ? plan->p.P : 0, n_objects, u, ld_u,
                                     plan ? plan->p.n_obs : 0);
     if (s != CUI_OK) return s;
-    cudaSetDevice(plan->p.device);
+    const cui::DeviceGuard dev_guard(plan->p.device);
     return cui::forward_device(&plan->p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects,
                                reinterpret_cast<float2*>(u), ld_u, static_cast<cudaStream_t>(stream));
 }
@@ -600,7 +638,7 @@ cui_status cui_born_adjoint(cui_born_plan* plan, const cui_complex32* u, int64_t
     cui_status s = cui::check_apply(plan, u, ld_u, plan ? plan->p.n_obs : 0, n_objects, gamma_hat, ld_gamma,
                                     plan ? plan->p.P : 0);
     if (s != CUI_OK) return s;
-    cudaSetDevice(plan->p.device);
+    const cui::DeviceGuard dev_guard(plan->p.device);
     return cui::adjoint_device(&plan->p, reinterpret_cast<const float2*>(u), ld_u, n_objects,
                                reinterpret_cast<float2*>(gamma_hat), ld_gamma, static_cast<cudaStream_t>(stream));
 }
@@ -611,7 +649,7 @@ cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t
                                     plan ? plan->p.P : 0);
     if (s != CUI_OK) return s;
     if (!u_meas || ld_u < plan->p.n_obs) return set_error(CUI_ERR_INVALID_ARG, "invalid u_meas");
-    cudaSetDevice(plan->p.device);
+    const cui::DeviceGuard dev_guard(plan->p.device);
     return cui::vjp_device(&plan->p, reinterpret_cast<const float2*>(gamma), ld_gamma,
                            reinterpret_cast<const float2*>(u_meas), ld_u, n_objects, reinterpret_cast<float2*>(grad),
                            ld_grad, loss, static_cast<cudaStream_t>(stream));
@@ -626,7 +664,7 @@ cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int6
     if (!u_meas || ld_u < plan->p.n_obs) return set_error(CUI_ERR_INVALID_ARG, "invalid u_meas");
     if (!lambda) return set_error(CUI_ERR_INVALID_ARG, "lambda is NULL");
     if (n_iter < 0 || !(step > 0.f)) return set_error(CUI_ERR_INVALID_ARG, "n_iter must be >= 0 and step > 0");
-    cudaSetDevice(plan->p.device);
+    const cui::DeviceGuard dev_guard(plan->p.device);
     return cui::lasso_device(&plan->p, reinterpret_cast<float2*>(gamma), ld_gamma, reinterpret_cast<const float2*>(u_meas),
                              ld_u, n_objects, step, lambda, n_iter, loss, static_cast<cudaStream_t>(stream));
 }
@@ -641,7 +679,7 @@ cui_status cui_born_timing_read(cui_born_plan* plan, cui_born_timing* out) {
     if (!plan || !out) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
     cui::Plan& p = plan->p;
     *out = cui_born_timing{0, 0, 0.0, 0.0};
-    cudaSetDevice(p.device);
+    const cui::DeviceGuard dev_guard(p.device);
     for (size_t i = 0; i < p.ev_used; ++i) {
         cudaError_t e = cudaEventSynchronize(p.ev_pool[2 * i + 1]);
         if (e != cudaSuccess) return cui::check_cuda(e, "cudaEventSynchronize");

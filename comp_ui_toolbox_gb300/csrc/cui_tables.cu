@@ -432,6 +432,7 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
         tmp.clear();
     };
     auto talloc = [&](void** ptr, size_t bytes) -> cudaError_t {
+        if (injected_alloc_failure(p)) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(ptr, std::max<size_t>(bytes, 1));
         if (e == cudaSuccess) tmp.push_back(*ptr);
         return e;
@@ -567,6 +568,7 @@ cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_object
 
 extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
                                                  cui_born_plan** plan) {
+    const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return
     return create_setup_plan(desc, max_objects, CUI_STORAGE_AUTO, nullptr, nullptr, plan);
 }
 
@@ -574,6 +576,7 @@ extern "C" cui_status cui_born_plan_create_setup_ex(const cui_born_setup_desc* d
                                                     int32_t storage, const char* cache_dir, cui_born_plan** plan,
                                                     int32_t* loaded) {
     if (loaded) *loaded = 0;
+    const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return
     return create_setup_plan(desc, max_objects, storage, cache_dir, loaded, plan);
 }
 
@@ -587,5 +590,6 @@ extern "C" cui_status cui_born_plan_create_setup_cached(const cui_born_setup_des
                                                         const char* cache_dir, cui_born_plan** plan, int32_t* loaded) {
     if (!cache_dir) return cui::set_error(CUI_ERR_INVALID_ARG, "cache_dir is NULL");
     if (loaded) *loaded = 0;
+    const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return
     return create_setup_plan(desc, max_objects, CUI_STORAGE_AUTO, cache_dir, loaded, plan);
 }

@@ -589,10 +589,18 @@ extern "C" cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precis
         plan->p.precision = 0;
         return CUI_OK;
     }
-    if (precision != CUI_PRECISION_BF16X3) return set_error(CUI_ERR_INVALID_ARG, "unknown precision");
-    cudaError_t e = cudaSetDevice(plan->p.device);
+    if (precision != CUI_PRECISION_BF16X3 && precision != CUI_PRECISION_BF16X3_FOLDED)
+        return set_error(CUI_ERR_INVALID_ARG, "unknown precision");
+    const DeviceGuard dev_guard(plan->p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     Plan& p = plan->p;
+    if (precision == CUI_PRECISION_BF16X3_FOLDED) {
+        cui_status s = phi_prepare(p);
+        if (s != CUI_OK) return s;
+        p.precision = 2;
+        return CUI_OK;
+    }
     if (!p.ws_status) {
         cui_status s = device_alloc(p, reinterpret_cast<void**>(&p.ws_status), sizeof(int));
         if (s != CUI_OK) return s;
@@ -606,12 +614,22 @@ extern "C" cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precis
     return CUI_OK;
 }
 
+extern "C" cui_status cui_born_set_wait_limit(cui_born_plan* plan, int64_t nanoseconds) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    if (nanoseconds < 0 || nanoseconds > 60000000000ll)
+        return set_error(CUI_ERR_INVALID_ARG, "wait limit must be 0 (default) or 1 ns to 60 s");
+    plan->p.wait_limit_ns = nanoseconds == 0 ? 1000000000ull : static_cast<uint64_t>(nanoseconds);
+    return CUI_OK;
+}
+
 extern "C" cui_status cui_born_plan_status(cui_born_plan* plan, int32_t* device_status) {
     using namespace cui;
     if (!plan || !device_status) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
     *device_status = 0;
     if (!plan->p.ws_status) return CUI_OK;
-    cudaError_t e = cudaSetDevice(plan->p.device);
+    const DeviceGuard dev_guard(plan->p.device);
+    cudaError_t e = dev_guard.err;
     if (e == cudaSuccess) e = cudaMemcpy(device_status, plan->p.ws_status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemset(plan->p.ws_status, 0, sizeof(int));
     if (e != cudaSuccess) return check_cuda(e, "status");

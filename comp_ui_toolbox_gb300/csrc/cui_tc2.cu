@@ -69,8 +69,8 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
 
 // wait by every lane of a producer warp; the result is made warp-uniform so that
 // the warp-wide tcgen05.ld that follows is always executed by all 32 lanes
-__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
-    const bool ok = tc::bar_wait_abortable(bar, parity, abort_flag, kWaitLimitNs);
+__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, uint64_t ns) {
+    const bool ok = tc::bar_wait_abortable(bar, parity, abort_flag, ns);
     return __all_sync(0xffffffffu, ok);
 }
 
@@ -144,6 +144,7 @@ struct Fwd2Args {
     int lines_per_group, n_lines;
     float2* part;  // [groups][S][B][E]
     int* status;
+    uint64_t wait_ns;  // limit of every wait for work (the drains keep kWaitLimitNs)
 };
 
 template <int NT>
@@ -243,14 +244,14 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             constexpr uint32_t id_hi = tc::idesc_bf16(128, 4 * NT), id_lo = tc::idesc_bf16(128, 2 * NT);
             for (int q = 0; q < Q; ++q) {
                 const int li = q / nKC, kc = q - li * nKC, bb = li & 1;
-                if (kc == 0 && !(ok = tc::bar_wait_abortable(BANDF + 8 * bb, (li >> 1) & 1, abort_flag, kWaitLimitNs)))
+                if (kc == 0 && !(ok = tc::bar_wait_abortable(BANDF + 8 * bb, (li >> 1) & 1, abort_flag, a.wait_ns)))
                     break;
                 const int s = q % C::NS;
-                if (!(ok = tc::bar_wait_abortable(FULL + 8 * s, (q / C::NS) & 1, abort_flag, kWaitLimitNs))) break;
+                if (!(ok = tc::bar_wait_abortable(FULL + 8 * s, (q / C::NS) & 1, abort_flag, a.wait_ns))) break;
                 const int k = q / kChainChunks, acc = static_cast<int>(static_cast<unsigned>(k) % C::NACC);
                 const bool first = (q % kChainChunks) == 0;
                 if (first && k >= C::NACC &&
-                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(k) / C::NACC) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(k) / C::NACC) - 1) & 1, abort_flag, a.wait_ns)))
                     break;
                 tc::fence_after_sync();
                 const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
@@ -298,13 +299,13 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                 // rows of line li+1 go into the buffer of line li-1 once its MMAs are done
                 if (kc == bpos && li >= 1 && li + 1 < nL) {
                     if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((li + 1) & 1), (((li + 1) >> 1) - 1) & 1, abort_flag,
-                                                      kWaitLimitNs)))
+                                                      a.wait_ns)))
                         break;
                     band(li + 1);
                 }
                 const int rs = q % C::NR;
                 if (q >= C::NR &&
-                    !(ok = tc::bar_wait_abortable(RAWE + 8 * rs, ((q / C::NR) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    !(ok = tc::bar_wait_abortable(RAWE + 8 * rs, ((q / C::NR) - 1) & 1, abort_flag, a.wait_ns)))
                     break;
                 const int x0 = kc * kKC;
                 const uint32_t seg = 8u * min(kKC, a.Nx - x0);
@@ -353,7 +354,7 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                 const int rs = q % C::NR, s = q % C::NS;
                 const int kc = q % nKC;
                 const int sl = tid & 15, g4s = tid >> 4;
-                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag))) break;
+                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag, a.wait_ns))) break;
                 const uint32_t raw = sRaw + rs * L.RS;
                 const bool xin = kc * kKC + 4 * g4s < a.Nx;
                 float4 pv[2], gv[4][2];
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                 }
                 tc::fence_async_smem();
                 tc::bar_arrive(RAWE + 8 * rs);
-                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag))) break;
+                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag, a.wait_ns))) break;
                 const uint32_t bst = sB + s * C::STB;
                 const float pr[4] = {pv[0].x, pv[0].z, pv[1].x, pv[1].z};
                 const float pi[4] = {pv[0].y, pv[0].w, pv[1].y, pv[1].w};
@@ -408,7 +409,7 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             } else if (q < Q) {
                 const int rs = q % C::NR, s = q % C::NS;
                 const int kc = q % nKC;
-                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag))) break;
+                if (!(ok = warp_wait(RAWF + 8 * rs, (q / C::NR) & 1, abort_flag, a.wait_ns))) break;
                 const uint32_t raw = sRaw + rs * L.RS;
                 float4 pv[C::ITEMS][2], gv[C::ITEMS][2];
 #pragma unroll
@@ -434,7 +435,7 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
                 // the generic-proxy reads above must be ordered before the next bulk copy (async proxy) into the stage
                 tc::fence_async_smem();
                 tc::bar_arrive(RAWE + 8 * rs);
-                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag))) break;
+                if (q >= C::NS && !(ok = warp_wait(EMPTY + 8 * s, ((q / C::NS) - 1) & 1, abort_flag, a.wait_ns))) break;
                 const uint32_t bst = sB + s * C::STB;
 #pragma unroll
                 for (int it = 0; it < C::ITEMS; ++it) {
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
             const int qr = q - C::LAG;
             if (qr >= 0 && (qr % kChainChunks == kChainChunks - 1 || qr == Q - 1)) {
                 const int k = qr / kChainChunks, accs = static_cast<int>(static_cast<unsigned>(k) % C::NACC);
-                if (!(ok = warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(k) / C::NACC) & 1, abort_flag))) break;
+                if (!(ok = warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(k) / C::NACC) & 1, abort_flag, a.wait_ns))) break;
                 tc::fence_after_sync();
                 const uint32_t col = tmem + lane_addr + static_cast<uint32_t>(accs * 4 * NT + h * NT);
 #pragma unroll
@@ -566,6 +567,7 @@ struct Adj2Args {
     int64_t P;
     float2* part;        // [nfc][B][P]
     int* status;
+    uint64_t wait_ns;  // limit of every wait for work (the drains keep kWaitLimitNs)
 };
 
 template <int NT>
@@ -686,13 +688,13 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             for (int u = 0; u < U; ++u) {
                 const int fi = u / upf, rem = u - fi * upf, zi = rem >> 2, r = rem & 3, kb = fi % C::NB;
                 if (zi == 0 && r == 0 &&
-                    !(ok = tc::bar_wait_abortable(BFULL + 8 * kb, (fi / C::NB) & 1, abort_flag, kWaitLimitNs)))
+                    !(ok = tc::bar_wait_abortable(BFULL + 8 * kb, (fi / C::NB) & 1, abort_flag, a.wait_ns)))
                     break;
                 const int sa = u % C::NA;
-                if (!(ok = tc::bar_wait_abortable(AFULL + 8 * sa, (u / C::NA) & 1, abort_flag, kWaitLimitNs))) break;
+                if (!(ok = tc::bar_wait_abortable(AFULL + 8 * sa, (u / C::NA) & 1, abort_flag, a.wait_ns))) break;
                 const int acc = static_cast<int>(static_cast<unsigned>(u) % C::NACC);
                 if (u >= C::NACC &&
-                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(u) / C::NACC) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    !(ok = tc::bar_wait_abortable(ACCE + 8 * acc, ((static_cast<unsigned>(u) / C::NACC) - 1) & 1, abort_flag, a.wait_ns)))
                     break;
                 tc::fence_after_sync();
                 const uint32_t td = tmem + static_cast<uint32_t>(acc * 4 * NT);
@@ -746,20 +748,20 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                 // V tile of frequency fi into the buffer of fi-NB once that frequency's MMAs are done
                 if (zi == 0 && r == 0 && fi >= C::NB) {
                     if (!(ok = tc::bar_wait_abortable(BEMPTY + 8 * (fi % C::NB), ((fi / C::NB) - 1) & 1, abort_flag,
-                                                      kWaitLimitNs)))
+                                                      a.wait_ns)))
                         break;
                     vtile(fi);
                 }
                 // rows of table row q+1 go into the buffer of q-1 once the producers have spread it
                 if (r == 0 && q >= 1 && q + 1 < nq) {
                     if (!(ok = tc::bar_wait_abortable(BANDE + 8 * ((q + 1) & 1), (((q + 1) >> 1) - 1) & 1, abort_flag,
-                                                      kWaitLimitNs)))
+                                                      a.wait_ns)))
                         break;
                     band(q + 1);
                 }
                 const int pu = u % C::NP;
                 if (u >= C::NP &&
-                    !(ok = tc::bar_wait_abortable(PE + 8 * pu, ((u / C::NP) - 1) & 1, abort_flag, kWaitLimitNs)))
+                    !(ok = tc::bar_wait_abortable(PE + 8 * pu, ((u / C::NP) - 1) & 1, abort_flag, a.wait_ns)))
                     break;
                 const int f = sF[fi];
                 const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
@@ -800,9 +802,9 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
         // ---- spread chunks of residue r of unit `it` -> A stage (threads t0 .. t0 + nthr - 1) ----
         auto spread = [&](int it, int t0, int nthr) -> bool {
             const int fi = it / upf, rem = it - fi * upf, zi = rem >> 2, r = rem & 3, q = fi * nL + zi, bb = q & 1;
-            if (r == 0 && !warp_wait(BANDF + 8 * bb, (q >> 1) & 1, abort_flag)) return false;
+            if (r == 0 && !warp_wait(BANDF + 8 * bb, (q >> 1) & 1, abort_flag, a.wait_ns)) return false;
             const int sa = it % C::NA;
-            if (it >= C::NA && !warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag)) return false;
+            if (it >= C::NA && !warp_wait(AEMPTY + 8 * sa, ((it / C::NA) - 1) & 1, abort_flag, a.wait_ns)) return false;
             const uint32_t as = sA + sa * L.AB;
             for (int idx = tid - t0; idx < 2 * NCH; idx += nthr) {
                 const int v = idx >= NCH ? 1 : 0, i = idx - v * NCH;
@@ -826,7 +828,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             const int f = sF[fi];
             const int ns = a.f_slot_ptr[f + 1] - a.f_slot_ptr[f];
             const bool xin = r + 4 * j < a.Nx;
-            if (!warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag)) return false;
+            if (!warp_wait(PF + 8 * pu, (ue / C::NP) & 1, abort_flag, a.wait_ns)) return false;
             float2 pv[NPS][MW];
 #pragma unroll
             for (int ps = 0; ps < NPS; ++ps)
@@ -841,7 +843,7 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
                 }
             tc::fence_async_smem();  // generic reads before the next bulk copy into this stage
             tc::bar_arrive(PE + 8 * pu);
-            if (!warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(ue) / C::NACC) & 1, abort_flag)) return false;
+            if (!warp_wait(ACCF + 8 * accs, (static_cast<unsigned>(ue) / C::NACC) & 1, abort_flag, a.wait_ns)) return false;
             tc::fence_after_sync();
 #pragma unroll
             for (int ps = 0; ps < NPS; ++ps) {
@@ -1047,7 +1049,7 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.S = p->S; a.B = B; a.Bt = t.Bt;
     a.ms = p->ms; a.P = p->P;
-    a.lines_per_group = lpg; a.n_lines = n_lines; a.part = p->ws_part; a.status = p->ws_status;
+    a.lines_per_group = lpg; a.n_lines = n_lines; a.part = p->ws_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
     const size_t smem = FwdLayout<NT>(a.ms, a.Bt, a.RBW).total;
     if ((e = cudaFuncSetAttribute(fwd_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem))) != cudaSuccess)
@@ -1082,7 +1084,7 @@ cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nf
     a.p_ad = p->p_ad; a.Jp = p->Jp; a.vs = p->ws_vs; a.tiles = t.tiles;
     a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list;
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.Epad = p->Epad; a.B = B; a.Bt = t.Bt; a.F = p->F;
-    a.fchunk = fchunk; a.ms = p->ms; a.L = Lz; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status;
+    a.fchunk = fchunk; a.ms = p->ms; a.L = Lz; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
     if ((e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(L.total))) != cudaSuccess)

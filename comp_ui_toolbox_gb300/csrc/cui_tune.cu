@@ -63,7 +63,8 @@ extern "C" cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, 
     Plan& p = plan->p;
     if (n_objects < 1 || n_objects > p.max_objects)
         return set_error(CUI_ERR_INVALID_ARG, "n_objects must be in [1, max_objects]");
-    cudaError_t e = cudaSetDevice(p.device);
+    const DeviceGuard dev_guard(p.device);
+    cudaError_t e = dev_guard.err;
     if (e != cudaSuccess) return check_cuda(e, "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t ng = static_cast<size_t>(p.P) * n_objects, nu = static_cast<size_t>(p.n_obs) * n_objects;

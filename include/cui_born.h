@@ -114,6 +114,13 @@ typedef struct {
     int64_t incident_bytes;         /* device bytes of all incident fields */
     int64_t workspace_bytes;        /* device scratch owned by the plan */
     int64_t contraction_macs;       /* complex MACs of one dense apply per object: sum_slots E*P */
+    int64_t channel_macs;           /* channel-contraction entries per object and dense apply:
+                                       sum_slots min(rows of the slot, distinct active elements) * P
+                                       (the element sum folded into the receive mixes) */
+    int64_t folded_bytes;           /* device bytes of the folded operator (0 until built) */
+    int64_t folded_sums;            /* distinct element sums the folded build formed */
+    int64_t device_allocations;     /* device allocations the plan has attempted so far (the count
+                                       CUI_BORN_FAIL_ALLOC=N refers to: the N-th of them fails) */
 } cui_born_info;
 
 /* ---- setup form: tables built on the device ---------------------------------
@@ -241,11 +248,15 @@ cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int
 /* Forward that allocates nothing.  No counterpart in the reference: its MEX
  * allocates device memory on every call.  Same operation and arguments as
  * cui_born_forward, for callers that must not allocate device memory when
- * they apply the operator (a stream being captured into a CUDA graph, plug-in
- * hosts with a fixed device-memory budget, real-time loops).  Partial sums
- * live in a 16 MiB file-scope device array that each GPU loading the library
- * holds until exit, so slots x n_objects x elements x 16 B must not exceed
- * 16 MiB (else CUI_ERR_INVALID_ARG).  The first call on a device looks up the
+ * they apply the operator: plug-in hosts that hand a plug-in a fixed
+ * device-memory budget and refuse further allocations, and real-time loops
+ * that must not enter the allocator (and its possible synchronisation)
+ * between frames.  It always runs the FP32 CUDA-core kernels, whatever
+ * cui_born_set_precision chose for the plan.  Partial sums live in a 16 MiB
+ * file-scope device array that each GPU loading the library holds until
+ * exit, so slots x n_objects x elements x 16 B must not exceed 16 MiB, and
+ * n_objects x (slot passes of the widest frequency) must not exceed 65535
+ * (else CUI_ERR_INVALID_ARG).  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before
  * any stream capture.  All calls share the array: calls that overlap on the
  * GPU (other streams, other plans, other threads) race. */
@@ -340,6 +351,22 @@ cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* y, int32_t 
 cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_complex64* input,
                                   int64_t ld_in, int32_t n_objects, cui_complex64* output, int64_t ld_out);
 
+/* Host LASSO: n_iter proximal-gradient iterations (as cui_born_lasso) on host FP64
+ * buffers: u_meas [N_obs x n_objects] (ld_u), gamma [N_points x n_objects]
+ * (ld_gamma) the start iterate on entry and the result on return, lambda [n_objects]
+ * thresholds in host memory.  Synchronous.  The MEX form of the solver loop that
+ * lq_minimization (operator.m:601-790) drives through combined_scalar (:717). */
+cui_status cui_born_lasso_host(cui_born_plan* plan, const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects,
+                               cui_complex64* gamma, int64_t ld_gamma, const float* lambda, float step,
+                               int32_t n_iter);
+
+/* How the host entry points move data: *direct = 1 when kernels read and write
+ * the caller's FP64 arrays through the host's page tables (GPUs with
+ * cudaDevAttrPageableMemoryAccessUsesHostPageTables, such as Grace systems), 0
+ * when the data pass through the plan's pinned staging buffers (also forced by
+ * CUI_BORN_HOST_STAGING=1 before the first host call). */
+cui_status cui_born_host_path(cui_born_plan* plan, int32_t* direct);
+
 /* Host VJP: same as cui_born_vjp with host FP64 buffers; loss may be NULL. */
 cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, int64_t ld_gamma,
                              const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects,
@@ -347,11 +374,26 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
 
 /* ---- precision ------------------------------------------------------------
  * CUI_PRECISION_FP32: FP32 CUDA-core contractions (default).
- * CUI_PRECISION_BF16X3: the adjoint contraction runs on the tcgen05 tensor
- * cores with every operand split into bf16 hi + lo and the three products
- * hi*hi + hi*lo + lo*hi accumulated in FP32 (2D setups, <= 128 elements).
- * Switching to BF16X3 builds the split band tables once (allocates). */
-typedef enum { CUI_PRECISION_FP32 = 0, CUI_PRECISION_BF16X3 = 1 } cui_precision;
+ * CUI_PRECISION_BF16X3: the forward and adjoint contractions over (slot,
+ * element) run on the tcgen05 tensor cores with every operand split into
+ * bf16 hi + lo and the three products hi*hi + hi*lo + lo*hi accumulated in
+ * FP32 (2D setups, <= 128 elements).  Switching to BF16X3 builds the split
+ * band tables once (allocates).
+ * CUI_PRECISION_BF16X3_FOLDED: the same split-BF16 arithmetic as two tcgen05
+ * GEMMs against the operator folded over its receive mixes and stored in
+ * device memory: one row per observation (w, m, f), sum over the mix's active
+ * elements of prefactor x table entry x incident field, the reference's
+ * per-element Phi matrices (combined_quick_gpu.cu:1099-1124) summed over e.
+ * It does min(mixes, active elements) / active elements of the element
+ * contraction's multiply-adds and reads 8 bytes per observation x grid point
+ * and apply direction (per 64-column pass); it needs a stored table and that
+ * much free device memory (CUI_ERR_UNSUPPORTED_SETUP otherwise).  Switching
+ * to it builds the matrix once (allocates).  Objects are applied 64 at a time. */
+typedef enum {
+    CUI_PRECISION_FP32 = 0,
+    CUI_PRECISION_BF16X3 = 1,
+    CUI_PRECISION_BF16X3_FOLDED = 2
+} cui_precision;
 
 cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precision);
 
@@ -391,6 +433,14 @@ typedef struct {
 } cui_born_timing;
 
 cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable);
+/* Wall-clock limit of every wait of the tensor-core kernels for an operand stage or an
+ * accumulator (no counterpart in the reference, whose kernels do not wait): a block
+ * whose wait runs out stops, drains its copies and MMAs (those drains keep a fixed
+ * 1 s limit), frees its tensor memory and raises the plan's status word, which
+ * cui_born_plan_status reports as CUI_ERR_TIMEOUT; blocks of later launches skip
+ * their work until the status is read.  nanoseconds = 0 restores the default of
+ * 1 s; otherwise 1 ns to 60 s. */
+cui_status cui_born_set_wait_limit(cui_born_plan* plan, int64_t nanoseconds);
 /* Reads and clears the plan's device status word; CUI_ERR_TIMEOUT when a
  * bounded device-side wait gave up since the last call. */
 cui_status cui_born_plan_status(cui_born_plan* plan, int32_t* device_status);

@@ -1,0 +1,82 @@
+"""Cleanup paths under device-allocation failures (GPU: plan creation allocates device memory).
+
+``CUI_BORN_FAIL_ALLOC=N`` makes the N-th device allocation of each plan fail as an out-of-memory
+error would (before cudaMalloc is called).  For every N up to the plan's allocation count, plan
+creation must return CUI_ERR_OOM and leave the device's free memory where it was; a precision
+switch that fails the same way must leave the plan working on its previous path.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import configs, forward_quick_cpu
+from tests.helpers import make_operator, rel_l2, setup_kwargs
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+SLACK = 4 << 20  # bytes of free-memory drift tolerated (driver bookkeeping)
+
+
+def _free():
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+@pytest.mark.parametrize("form", ["table", "setup"])
+def test_every_failed_allocation_of_plan_creation_is_clean(form, monkeypatch):
+    from comp_ui_toolbox_gb300 import CuiError, OperatorBorn
+    b = configs.build(configs.small_config("c2"))
+    create = (lambda: make_operator(b, "lateral", max_objects=4)) if form == "table" else \
+        (lambda: OperatorBorn.from_setup(**setup_kwargs(b.cfg), device=0, max_objects=4))
+    create().close()  # warm: first-use allocations of the runtime are outside the measurement
+    free0 = _free()
+    n = 1
+    while n < 200:
+        monkeypatch.setenv("CUI_BORN_FAIL_ALLOC", str(n))
+        try:
+            op = create()
+        except CuiError as e:
+            assert e.status == 3, e
+            assert "injected allocation failure" in str(e)
+            assert abs(_free() - free0) <= SLACK, n
+            n += 1
+            continue
+        break
+    monkeypatch.delenv("CUI_BORN_FAIL_ALLOC")
+    assert n > 5  # several allocations were failed one at a time
+    gamma = configs.make_gamma(b.cfg)
+    u = op.forward(torch.from_numpy(gamma.astype(np.complex64)).cuda()).cpu().numpy()
+    assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= 1e-5
+    op.close()
+    assert abs(_free() - free0) <= SLACK
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16x3-folded"])
+def test_failed_precision_switch_keeps_the_plan_working(precision, monkeypatch):
+    """Fail the j-th allocation of the switch for j = 1, 2, ... until it succeeds."""
+    from comp_ui_toolbox_gb300 import CuiError
+    b = configs.build(configs.small_config("c2"))
+    op = make_operator(b, "lateral", max_objects=4)
+    gamma = configs.make_gamma(b.cfg)
+    g = torch.from_numpy(gamma.astype(np.complex64)).cuda()
+    u_ref = forward_quick_cpu(b.op, gamma)
+    failures = 0
+    for j in range(1, 100):
+        n0 = op.refresh_info()["device_allocations"]
+        monkeypatch.setenv("CUI_BORN_FAIL_ALLOC", str(n0 + j))
+        try:
+            op.set_precision(precision)
+        except CuiError as e:
+            assert e.status == 3
+            failures += 1
+            monkeypatch.delenv("CUI_BORN_FAIL_ALLOC")
+            assert rel_l2(op.forward(g).cpu().numpy(), u_ref) <= 1e-5  # still the previous path
+            continue
+        break
+    monkeypatch.delenv("CUI_BORN_FAIL_ALLOC", raising=False)
+    assert failures >= 1
+    assert op.precision == precision  # a later switch built what the failed ones could not
+    assert rel_l2(op.forward(g).cpu().numpy(), u_ref) <= 1e-5
+    assert op.device_status() == 0
+    op.close()
