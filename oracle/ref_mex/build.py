@@ -59,7 +59,9 @@ def build(reference: Path = DEFAULT_REFERENCE, force: bool = False) -> Path | No
           "-o", str(cs)])
     _run(["g++", "-std=c++17", "-O2", "-fPIC", f"-I{HERE}", "-c", str(HERE / "mex_stub.cpp"), "-o", str(ms)])
     tmp = LIB.with_suffix(".so.tmp")
-    _run(["g++", "-shared", "-o", str(tmp), str(gw), str(cs), str(ms)])
+    # -Bsymbolic: the gateway's CUDA, cuBLAS and MEX calls bind to the stand-ins linked here, never to a
+    # real CUDA runtime another library of the process has loaded
+    _run(["g++", "-shared", "-Wl,-Bsymbolic", "-o", str(tmp), str(gw), str(cs), str(ms)])
     os.replace(tmp, LIB)
     return LIB
 

@@ -1,8 +1,9 @@
-/* Minimal MATLAB MEX API for running the reference's MEX gateway outside MATLAB.
+/* Minimal MATLAB MEX API for running MEX gateways outside MATLAB.
  *
- * TEST INFRASTRUCTURE ONLY (the oracle's reference runner, oracle/ref_mex/): declares the
- * mx and mex functions that +scattering/combined_quick_gpu.cu calls, implemented by
- * mex_stub.cpp over an in-memory property tree that the runner fills from Python.
+ * TEST INFRASTRUCTURE ONLY (oracle/ref_mex/): declares the mx and mex functions that the
+ * reference's +scattering/combined_quick_gpu.cu and this library's gateways
+ * (comp_ui_toolbox_gb300/mex/) call, implemented by mex_stub.cpp over an in-memory property
+ * tree that the runners fill from Python.
  * Interleaved complex storage (R2018a API, combined_quick_gpu.m:32). */
 #ifndef CUI_REF_MEX_H
 #define CUI_REF_MEX_H
@@ -47,6 +48,7 @@ void* mxRealloc(void* ptr, size_t size);
 void mxFree(void* ptr);
 void mexErrMsgIdAndTxt(const char* id, const char* fmt, ...);
 int mexPrintf(const char* fmt, ...);
+int mexAtExit(void (*fn)(void));
 /* the gateway every MEX file defines (C linkage, as MATLAB's header declares it) */
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]);
 

@@ -39,6 +39,7 @@ bool g_in_call = false;
 char g_err_id[256];
 char g_err_msg[512];
 bool g_verbose = false;
+void (*g_at_exit)(void) = nullptr;
 
 mxArray* fresh() {
     g_arena.emplace_back(new mxArray());
@@ -161,6 +162,11 @@ void mexErrMsgIdAndTxt(const char* id, const char* fmt, ...) {
     fail(id, msg);
 }
 
+int mexAtExit(void (*fn)(void)) {
+    g_at_exit = fn;
+    return 0;
+}
+
 int mexPrintf(const char* fmt, ...) {
     if (!g_verbose) return 0;
     va_list ap;
@@ -210,11 +216,13 @@ int ref_set_cell(mxArray* cell, size_t index, mxArray* value) {
     return 0;
 }
 
-// Runs the gateway: output = combined_quick_gpu(operator, mode, input).  Returns 0 and the
-// output node, or 1 with the error identifier and message of mexErrMsgIdAndTxt.
-int ref_call(const mxArray* op, const mxArray* mode, const mxArray* input, int nrhs, mxArray** out, char* err_id,
-             size_t err_id_len, char* err_msg, size_t err_msg_len) {
-    const mxArray* prhs[3] = {op, mode, input};
+// Runs the gateway with nrhs (<= 16) inputs and one output, as MATLAB would: returns 0 and the
+// output node, or 1 with the error identifier and message of mexErrMsgIdAndTxt.  ref_call is the
+// three-input form output = combined_quick_gpu(operator, mode, input).
+int ref_call_args(const mxArray* const* args, int nrhs, mxArray** out, char* err_id, size_t err_id_len, char* err_msg,
+                  size_t err_msg_len) {
+    const mxArray* prhs[16] = {nullptr};
+    for (int i = 0; i < nrhs && i < 16; ++i) prhs[i] = args[i];
     mxArray* plhs[1] = {nullptr};
     g_err_id[0] = g_err_msg[0] = '\0';
     g_in_call = true;
@@ -229,6 +237,12 @@ int ref_call(const mxArray* op, const mxArray* mode, const mxArray* input, int n
     std::snprintf(err_msg, err_msg_len, "%s", g_err_msg);
     *out = nullptr;
     return 1;
+}
+
+int ref_call(const mxArray* op, const mxArray* mode, const mxArray* input, int nrhs, mxArray** out, char* err_id,
+             size_t err_id_len, char* err_msg, size_t err_msg_len) {
+    const mxArray* args[3] = {op, mode, input};
+    return ref_call_args(args, nrhs, out, err_id, err_id_len, err_msg, err_msg_len);
 }
 
 int ref_dims(const mxArray* a, size_t* m, size_t* n, int* is_complex) {
@@ -246,6 +260,11 @@ int ref_read(const mxArray* a, double* out) {
 }
 
 void ref_reset(void) { g_arena.clear(); }
+// what MATLAB does when the MEX file is cleared: the function registered by mexAtExit runs
+void ref_clear_mex(void) {
+    if (g_at_exit) g_at_exit();
+    g_at_exit = nullptr;
+}
 void ref_verbose(int on) { g_verbose = on != 0; }
 
 }  // extern "C"

@@ -1,4 +1,4 @@
-"""The reference's own MEX gateway, run on the host: ``combined_quick_gpu(operator_born, mode, x)``.
+"""MEX gateways run on the host: the reference's ``combined_quick_gpu(operator_born, mode, x)``.
 
 TEST INFRASTRUCTURE ONLY: it pins the oracle (and, through fixtures, the device path) to the
 reference's own code.  ``oracle/ref_mex/build.py`` compiles ``+scattering/combined_quick_gpu.cu``
@@ -17,6 +17,10 @@ that the gateway reads (``combined_quick_gpu.cu:203-393`` and ``:817-823``) from
 All indices are 1-based doubles and all matrices column-major, as MATLAB passes them.
 Requires the symmetric representation (``h_ref`` + ``shift``), i.e. a field of view at least as
 wide as the array; narrower ones have no valid ``indices_grid_FOV_shift`` in the reference.
+The object also carries the grid geometry (``setup.FOV.shape.grid.N_points_axis``,
+``setup.xdc_array.N_elements_axis``, ``setup.N_points_per_pitch_axis``) that this library's own
+MEX gateways (``comp_ui_toolbox_gb300/mex/``) read; ``ReferenceGateway(path)`` loads any gateway
+linked with ``oracle/ref_mex/mex_stub.cpp``.
 """
 
 from __future__ import annotations
@@ -55,7 +59,9 @@ class ReferenceGateway:
         lib.ref_call.argtypes = [vp, vp, vp, C.c_int, C.POINTER(vp), C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t]
         lib.ref_dims.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_int)]
         lib.ref_read.argtypes = [vp, vp]
-        lib.ref_kernel_launches.restype = C.c_int
+        lib.ref_call_args.argtypes = [vp, C.c_int, C.POINTER(vp), C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t]
+        if hasattr(lib, "ref_kernel_launches"):
+            lib.ref_kernel_launches.restype = C.c_int
         self.lib = lib
 
     # ---- nodes -------------------------------------------------------------------------
@@ -109,7 +115,17 @@ class ReferenceGateway:
         self.set(setup, "indices_grid_FOV_shift", self.dbl(np.asarray(op.shift, dtype=float)))
         xdc = self.obj("scattering.sequences.setups.transducers.array_planar_regular_orthogonal")
         self.set(xdc, "N_elements", self.dbl(float(E)))
+        self.set(xdc, "N_elements_axis", self.dbl(np.asarray(op.setup.n_elements_axis, dtype=float)))
         self.set(setup, "xdc_array", xdc)
+        # grid geometry (not read by the reference's gateway; read by this library's gateways)
+        self.set(setup, "N_points_per_pitch_axis", self.dbl(np.asarray(op.setup.ppp_axis, dtype=float).reshape(1, -1)))
+        grid = self.obj("math.grid_regular_orthogonal")
+        self.set(grid, "N_points_axis", self.dbl(np.asarray(op.setup.n_points_axis, dtype=float).reshape(1, -1)))
+        shape = self.obj("scattering.sequences.setups.geometry.orthotope")
+        self.set(shape, "grid", grid)
+        fov = self.obj("scattering.sequences.setups.fields_of_view.field_of_view")
+        self.set(fov, "shape", shape)
+        self.set(setup, "FOV", fov)
         self.set(seq, "setup", setup)
         self.set(ob, "indices_measurement_sel", self.dbl(np.arange(1, W + 1, dtype=float).reshape(1, -1)))
         settings = self.obj("scattering.sequences.settings.setting", W)
@@ -151,9 +167,15 @@ class ReferenceGateway:
 
     def call_nodes(self, op_node, mode_node, x_node, nrhs: int = 3) -> np.ndarray:
         """The same with every argument given as a node (``obj``, ``cell``, ``dbl``)."""
+        return self.call_args([op_node, mode_node, x_node], nrhs)
+
+    def call_args(self, nodes, nrhs: int | None = None) -> np.ndarray:
+        """A gateway call with any number of input nodes and one output."""
+        arr = (C.c_void_p * max(1, len(nodes)))(*nodes)
         out = C.c_void_p()
         eid, emsg = C.create_string_buffer(256), C.create_string_buffer(512)
-        if self.lib.ref_call(op_node, mode_node, x_node, nrhs, C.byref(out), eid, 256, emsg, 512) != 0:
+        n = len(nodes) if nrhs is None else nrhs
+        if self.lib.ref_call_args(arr, n, C.byref(out), eid, 256, emsg, 512) != 0:
             raise RefMexError(eid.value.decode(), emsg.value.decode())
         m, n, c = C.c_size_t(), C.c_size_t(), C.c_int()
         if self.lib.ref_dims(out, C.byref(m), C.byref(n), C.byref(c)) != 0:
