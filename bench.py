@@ -51,9 +51,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--fp32-steps", type=int, default=3,
                     help="steps of the plain FP32 path timed after the main region (0: skip)")
-    ap.add_argument("--precision", choices=["fp32", "bf16x3", "auto"], default=None,
-                    help="contraction path: FP32 CUDA cores, split-BF16 tcgen05 tensor cores, or the per-plan "
-                         "autotuner (default: bf16x3 for 2d-batched, fp32 for 3d, auto otherwise)")
+    ap.add_argument("--precision", choices=["fp32", "bf16x3", "bf16x3-folded", "auto"], default=None,
+                    help="contraction path: FP32 CUDA cores, split-BF16 tcgen05 tensor cores over slots and "
+                         "elements, split-BF16 tcgen05 GEMMs against the folded operator stored in device memory, "
+                         "or the per-plan autotuner (default: bf16x3-folded for 2d-batched, fp32 for 3d, auto "
+                         "otherwise)")
     ap.add_argument("--table-storage", choices=["auto", "stored", "streamed", "generated"], default=None,
                     help="lateral transfer-function table: stored once; regenerated every apply in chunks of "
                          "frequencies (streamed, 3D); or generated inside the contraction kernels where they use "
@@ -74,6 +76,50 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return world, rank, local
+
+
+# ---- replicas (one process per GPU; the path needs no data exchange for this metric) --------
+def replicas_begin(world: int, backend: str = "nccl"):
+    """Process group of the replicas (torchrun's env:// rendezvous); None for one process."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend)
+    return dist
+
+
+def replicas_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def replicas_max_ms(dist, ms: float, device=None) -> float:
+    """The slowest replica's timed region: every replica waits for it, so it is the job's time."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_replica: float, ms: float) -> float:
+    """Units all replicas processed per second of the slowest replica's time (weak scaling)."""
+    return world * units_per_replica / (ms / 1e3)
+
+
+def replicas_end(dist):
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def relaunch_as_replicas(n: int) -> int:
+    """``--gpus N`` outside torchrun: run this command as N replica processes under
+    torch.distributed.run (rendezvous on 127.0.0.1) and return its exit code."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29511"),
+           str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
 
 
 def peaks():
@@ -135,60 +181,91 @@ def time_greedy(op):
             "data": "16 seeded point scatterers, noiseless"}
 
 
-def roofline_of(args, info, kt, B, clk):
+def roofline_of(args, info, kt, B, clk, p_used: float = 1.0):
     """Roofline of the dominant contraction kernel of one apply.
 
-    Split-BF16 (tensor cores): algorithmic work = 24 FLOP per complex MAC
-    (4 real products x 3 bf16 products x 2) over the S*P*E complex MACs of a
-    dense apply, padding excluded, against the measured bf16 tensor peak.
-    FP32 (CUDA cores): 8 FLOP per complex MAC against 152 SMs x 128 lanes x 2 x
-    the sampled SM clock.  Both carry the HBM view (compulsory bytes: incident
-    fields, transfer-function table, gamma and the output, once per launch).
+    Algorithmic work (the survey's work count): E = sum over slots of min(rows of the slot,
+    distinct active elements) x P_used complex multiply-adds per object (``channel_macs``:
+    the element sum folded into the receive mixes; P_used = the union occupancy of the
+    forward's gamma columns, all points for the adjoint), x B objects.
+
+    Split-BF16 (tensor cores): 24 FLOP per complex MAC (4 real products x 3 bf16 products
+    x 2) against the measured bf16 tensor peak.  The folded-operator GEMMs stream the
+    stored matrix (8 B per entry and launch) at 192 FLOP per byte, below the ridge point
+    (peak FLOP/s / peak B/s), so their governing roof is HBM: ``bound`` "hbm" with the
+    bytes one launch must move (matrix + operands + outputs) and the tensor figure beside.
+    FP32 (CUDA cores): 8 FLOP per complex MAC against 152 SMs x 128 lanes x 2 x the sampled
+    SM clock.  ``executed_*`` counts the multiply-adds the kernel actually performs (the
+    element contraction: S x E x P, all points).
     """
     pk = peaks()
-    macs = info["contraction_macs"] * B
     dom = "forward" if kt["ms_forward"] >= kt["ms_adjoint"] else "adjoint"
     t_launch = kt["ms_" + dom] / max(1, kt["n_" + dom]) / 1e3
     P = info["n_points"]
+    folded = args.precision == "bf16x3-folded"
+    alg_macs = info["channel_macs"] * B * (p_used if dom == "forward" else 1.0)
+    exec_macs = (info["channel_macs"] if folded else info["contraction_macs"]) * B
     # table bytes one launch moves: a stored table is read once; a streamed one is written by the chunk
     # generator and read back (the full table, chunk by chunk); a generated one never leaves the SMs
     table = {"stored": info["table_bytes"], "streamed": 2 * args.full_table_bytes, "generated": 0}[args.table_used]
-    compulsory = table + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
+    if folded:
+        compulsory = info["folded_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
+    else:
+        compulsory = table + info["incident_bytes"] + 8 * B * P + 8 * B * info["n_observations"]
     tc = args.precision != "fp32"
     # every 2D benchmark workload (4 grid points per pitch, lines a multiple of 8) runs the line-unit kernels;
     # 3D setups run the FP32 kernels under register ceilings (dense3) or with the generator inside (gen)
     fp32_kind = "dense" if args.n_dims == 2 else ("gen" if args.table_used == "generated" else "dense3")
     kernel = {("forward", True): "fwd_tc2_kernel", ("adjoint", True): "adj_tc2_kernel",
               ("forward", False): f"fwd_{fp32_kind}_kernel", ("adjoint", False): f"adj_{fp32_kind}_kernel"}[(dom, tc)]
+    if folded:
+        kernel = "phi_gemm_kernel<" + ("true" if dom == "adjoint" else "false") + ">"
     traffic = launch_traffic(args.workload, kernel, args.n_freq_used)
     hbm = {"compulsory_bytes": compulsory, "achieved_gbs": compulsory / t_launch / 1e9,
            "peak_gbs": pk["hbm_gbs"], "frac": compulsory / t_launch / 1e9 / pk["hbm_gbs"],
            "traffic_over_compulsory": (traffic / compulsory) if traffic else None}
     # the reference writes Phi (8 B per complex entry) and reads it back through cublasCgemm: the
     # rate at which this launch covers those bytes, against the HBM peak (the plain-FP32 criterion)
-    hbm["phi_equivalent_gbs"] = 8.0 * macs / t_launch / 1e9
+    hbm["phi_equivalent_gbs"] = 8.0 * alg_macs / t_launch / 1e9
     hbm["phi_equivalent_frac"] = hbm["phi_equivalent_gbs"] / pk["hbm_gbs"]
     sm_mhz = clk.get("sm_mhz") or pk["sm_max_mhz"]
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     launch_ms = {"forward": kt["ms_forward"] / max(1, kt["n_forward"]),
                  "adjoint": kt["ms_adjoint"] / max(1, kt["n_adjoint"])}
+    work = {"algorithmic_complex_macs_per_launch": alg_macs, "executed_complex_macs_per_launch": exec_macs,
+            "p_used_fraction": p_used if dom == "forward" else 1.0,
+            "definition": "E = sum over slots of min(rows, distinct active elements) x P_used per object "
+                          "(channel_macs), x objects; P_used = union occupancy of the forward's gamma"}
+    peak_src = (f"{pk['source']} bf16 burst (MEASURED_PEAKS.json bf16_tflops)" if pk["source"] == "measured"
+                else "fallback")
     if tc:
-        flops = 24.0 * macs
+        flops = 24.0 * alg_macs
         achieved = flops / t_launch / 1e12
-        return {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / pk["bf16_tflops"], "traffic": traffic, "kernel": kernel,
-                "peak_source": f"{pk['source']} bf16 burst (MEASURED_PEAKS.json bf16_tflops)"
-                               if pk["source"] == "measured" else "fallback",
-                "achieved_definition": "24 FLOP per complex MAC (4 real x 3 split-BF16 products x 2) x S*P*E "
-                                       "complex MACs per launch (padding excluded) / average launch time",
-                "flops_per_launch": flops, "hbm": hbm, "launch_ms": launch_ms}
-    flops = 8.0 * macs
+        tensor = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                  "frac": achieved / pk["bf16_tflops"], "peak_source": peak_src,
+                  "executed_tflops": 24.0 * exec_macs / t_launch / 1e12,
+                  "achieved_definition": "24 FLOP per complex MAC (4 real x 3 split-BF16 products x 2) x the "
+                                         "algorithmic complex MACs per launch / average launch time"}
+        if folded:
+            return {"bound": "hbm", "achieved": hbm["achieved_gbs"], "peak": pk["hbm_gbs"], "unit": "GB/s",
+                    "frac": hbm["frac"], "traffic": traffic, "kernel": kernel,
+                    "peak_source": "measured HBM copy (MEASURED_PEAKS.json hbm_gbs)" if pk["source"] == "measured"
+                    else "fallback",
+                    "achieved_definition": "bytes one launch must move (folded matrix, 8 B per observation x point, "
+                                           "+ gamma and observations in FP32) / average launch time; the GEMM runs "
+                                           "at 192 FLOP/B, below the bf16 ridge point, so HBM governs",
+                    "tensor": tensor, "work": work, "hbm": hbm, "launch_ms": launch_ms}
+        return dict(tensor, traffic=traffic, kernel=kernel, work=work, hbm=hbm, launch_ms=launch_ms,
+                    flops_per_launch=flops)
+    flops = 8.0 * alg_macs
     achieved = flops / t_launch / 1e12
     return {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak, "traffic": traffic, "kernel": kernel,
             "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median sampled SM clock",
-            "achieved_definition": "8 FLOP per complex MAC x S*P*E complex MACs per launch / average launch time",
-            "flops_per_launch": flops, "hbm": hbm, "launch_ms": launch_ms}
+            "achieved_definition": "8 FLOP per complex MAC x the algorithmic complex MACs per launch / average "
+                                   "launch time",
+            "executed_tflops": 8.0 * exec_macs / t_launch / 1e12,
+            "flops_per_launch": flops, "work": work, "hbm": hbm, "launch_ms": launch_ms}
 
 
 class ClockSampler:
@@ -257,10 +334,17 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# bounded CPU sample per workload (waves, frequencies, receive mixes): about 10-30 s of host work
-# bounded CPU samples: (waves, frequencies, receive mixes or None = all, axial planes or None = all)
-CPU_SAMPLE = {"2d-plain": (1, 8, None, None), "2d-gradient": (1, 8, None, None), "2d-batched": (1, 1, 8, None),
+# bounded CPU samples (about 10-30 s of host work): (waves, frequencies, receive mixes or None = all,
+# axial planes or None = all); "cores" = one receive mix per host core (the 32 mixes of 2d-batched)
+CPU_SAMPLE = {"2d-plain": (1, 8, None, None), "2d-gradient": (1, 8, None, None), "2d-batched": (1, 1, "cores", None),
               "3d": (1, 1, None, 4)}
+# per-step samples of the reference arm, small enough for --steps K --warmup W to end within minutes
+REF_SAMPLE = {"2d-plain": (1, 2, None, None), "2d-gradient": (1, 1, None, 128), "2d-batched": (1, 1, "cores", 128),
+              "3d": (1, 1, None, 2)}
+
+
+def sample_mixes(nm):
+    return min(32, max(8, os.cpu_count() or 8)) if nm == "cores" else nm
 
 
 def cpu_baseline(workload: str, n_objects: int, op=None, w=None):
@@ -271,8 +355,8 @@ def cpu_baseline(workload: str, n_objects: int, op=None, w=None):
     the first column of the adjoint of exactly those rows."""
     from oracle.cpu_baseline import time_sample
     nw, nf, nm, npl = CPU_SAMPLE[workload]
-    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=nm, n_planes=npl,
-                    check=op is not None)
+    r = time_sample(ORACLE_NAME[workload], n_waves=nw, n_freq=nf, n_objects=n_objects, n_mixes=sample_mixes(nm),
+                    n_planes=npl, check=op is not None)
     out = {"value": r["applies_per_s"], "unit": "applies/s", "cores": r["cores"], "kind": "port",
            "sample": r["sample"], "seconds_sample": r["seconds_sample"]}
     check = None
@@ -324,24 +408,39 @@ def workload_config(w, B):
 
 
 def run_reference(args):
+    """The reference's CPU operator (its FP64 restatement, the oracle port) on the host cores.
+
+    Every step times one forward + adjoint over a bounded sample of the workload (``REF_SAMPLE``,
+    split over one spawn process per host core); ``warmup`` + ``steps`` such samples run and
+    ``ms_per_step`` is the median sample step as measured.  ``value`` scales that step to the
+    full workload (linear in waves x frequencies x mixes x grid points): the line says so with
+    ``extrapolated`` and ``scale_factor``.
+    """
     world, rank, _ = dist_env()
     if rank != 0:
         return
     from comp_ui_toolbox_gb300.workloads import workload
-    w = workload(args.workload)
+    w = workload(args.workload if args.workload in ORACLE_NAME else "2d-gradient")
     B = w.n_objects if args.workload == "2d-batched" else 1
     from oracle.cpu_baseline import time_sample
-    nw, nf, nm, npl = CPU_SAMPLE[args.workload]
-    first = time_sample(ORACLE_NAME[args.workload], n_waves=nw, n_freq=nf, n_objects=B, n_mixes=nm, n_planes=npl,
-                        repeats=max(1, min(3, args.warmup + args.steps)))
-    t_full = first["seconds_full_apply"]
-    value = first["applies_per_s"]
+    nw, nf, nm, npl = REF_SAMPLE[w.name]
+    t0 = time.perf_counter()
+    r = time_sample(ORACLE_NAME[w.name], n_waves=nw, n_freq=nf, n_objects=B, n_mixes=sample_mixes(nm),
+                    n_planes=npl, repeats=args.warmup + args.steps)
+    wall = time.perf_counter() - t0
+    timed = sorted(r["seconds_per_repeat"][args.warmup:])
+    t_step = timed[len(timed) // 2]
+    value = B / (t_step * r["scale"])
     line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_full * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": workload_config(w, B),
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": first["cores"], "kind": "port",
-                             "sample": first["sample"]},
+            "extrapolated": True, "scale_factor": r["scale"],
+            "step_definition": "one forward + adjoint of the bounded sample below (ms_per_step as measured, median "
+                               "of the timed steps); value = objects / (sample step seconds x scale_factor)",
+            "wall_s": wall,
+            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": r["cores"], "kind": "port",
+                             "host_cores": os.cpu_count(), "sample": r["sample"]},
             "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -351,9 +450,7 @@ def run_ours(args):
     import torch
 
     world, rank, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = replicas_begin(world)
     torch.cuda.set_device(local)
     from comp_ui_toolbox_gb300 import OperatorBorn, launch_count
     from comp_ui_toolbox_gb300.workloads import workload
@@ -372,24 +469,39 @@ def run_ours(args):
     args.full_table_bytes = full_table_bytes(w)
     P, N = op.n_points, op.n_observations
 
-    # data: u = Phi gamma_true + 30 dB noise; the gradient is taken at a seeded Gaussian gamma
+    # data: u = Phi gamma_true + 30 dB noise.  The batched workload takes the gradient at its own
+    # configured right-hand sides (64 further columns at 3 % Gaussian sparsity, independent seeds);
+    # the single-object workloads at a seeded Gaussian gamma (the gradient point of 2d-gradient)
     gamma_true = torch.from_numpy(w.gamma(n_objects=B).astype(np.complex64)).cuda()
     u_clean = op.forward(gamma_true)
     gen = torch.Generator(device="cuda").manual_seed(7)
     noise = torch.randn(u_clean.shape, dtype=torch.complex64, device="cuda", generator=gen)
     snr = 10 ** (-30 / 20)
     u_meas = (u_clean + noise * (u_clean.abs().pow(2).mean().sqrt() / noise.abs().pow(2).mean().sqrt()) * snr).contiguous()
-    gamma = torch.randn((P, B), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
+    if args.workload == "2d-batched":
+        gamma = torch.from_numpy(w.gamma(seed=w.seed + 1, n_objects=B).astype(np.complex64)).cuda()
+        gamma_kind = f"{B} columns at {w.density:.0%} Gaussian sparsity (independent seeds)"
+    else:
+        gamma = torch.randn((P, B), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
+        gamma_kind = "seeded Gaussian (dense)"
+    # union occupancy of the forward's columns: the reference's forward contracts only these points
+    p_used = float((gamma.abs().amax(dim=1) > 0).float().mean())
     autotune = None
     if args.precision == "auto":  # the per-plan autotuner keeps the faster path; the bench then runs that
         autotune = op.autotune(B)
         args.precision = autotune["precision"]
     accuracy = None
+    t_fold = None
     if args.precision != "fp32":
         # same plan, both precisions: relative L2 of the split-BF16 gradient against the FP32 one
         op.set_precision("fp32")
         g32, _ = op.vjp(gamma, u_meas)
+        t0 = time.perf_counter()
         op.set_precision(args.precision)
+        torch.cuda.synchronize()
+        if args.precision == "bf16x3-folded":
+            t_fold = time.perf_counter() - t0
+        op.refresh_info()
         gtc, _ = op.vjp(gamma, u_meas)
         accuracy = {"rel_l2_grad_vs_fp32": float((gtc - g32).norm() / g32.norm()),
                     "note": "the FP32 path itself is <= 2e-7 from the FP64 oracle on the test workloads"}
@@ -402,8 +514,7 @@ def run_ours(args):
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        replicas_barrier(dist)
         stream = torch.cuda.current_stream()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         op.timing(True)
@@ -417,18 +528,13 @@ def run_ours(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         clocks.mark_end()
-    if world > 1:
-        dist.barrier()
+    replicas_barrier(dist)
     launches = launch_count() - n0
     kt = op.timing()
     op.timing(False)
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas_max_ms(dist, ev0.elapsed_time(ev1), device="cuda")
     ms_step = ms / args.steps
-    value = world * args.steps * B / (ms / 1e3)
+    value = whole_job_rate(world, args.steps * B, ms)
 
     # end to end through the host (FP64) entry point: copies inside the timed region
     e2e_steps = args.e2e_steps or max(1, min(args.steps, 5))
@@ -442,13 +548,18 @@ def run_ours(args):
     for _ in range(e2e_steps):
         grad_h, loss_h = op.vjp(g_host, u_host, out=grad_out)
     t_e2e = time.perf_counter() - t0
+    host_path = op.host_path()
     e2e = {"value": e2e_steps * B / t_e2e, "unit": "applies/s",
-           "h2d_bytes_per_step": 8 * (P + N) * B, "d2h_bytes_per_step": 8 * P * B + 4 * B,
-           "path": "cui_born_vjp_host: FP64 host buffers -> FP32 pinned staging -> H2D -> VJP -> D2H -> FP64"}
+           "h2d_bytes_per_step": 16 * (P + N) * B, "d2h_bytes_per_step": 16 * P * B + 8 * B,
+           "path": ("cui_born_vjp_host: the caller's FP64 host arrays read and written by device kernels through "
+                    "the host page tables (Grace ATS over NVLink-C2C), VJP on the device in between"
+                    if host_path == "direct" else
+                    "cui_born_vjp_host: FP64 host buffers -> FP32 pinned staging -> H2D -> VJP -> D2H -> FP64"),
+           "bytes": "FP64 complex host data crossing host<->device per step (gamma and u in, gradient and loss out)"}
 
     # roofline of the dominant contraction kernel
     clk = clocks.summary()
-    roofline = roofline_of(args, op.info, kt, B, clk)
+    roofline = roofline_of(args, op.info, kt, B, clk, p_used)
     info = op.info
     macs = info["contraction_macs"] * B
 
@@ -459,7 +570,12 @@ def run_ours(args):
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "clocks": clk,
             "plan": {"build_s": t_build, "table_storage": op.table_storage,
                      "table_bytes": info["table_bytes"], "incident_bytes": info["incident_bytes"],
-                     "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs},
+                     "workspace_bytes": info["workspace_bytes"], "complex_macs_per_apply": macs,
+                     "channel_macs_per_apply": info["channel_macs"] * B,
+                     "folded_bytes": info["folded_bytes"], "folded_sums": info["folded_sums"],
+                     "folded_build_s": t_fold},
+            "inputs": {"gamma": gamma_kind, "p_used_fraction": p_used,
+                       "u": "Phi gamma_true + complex Gaussian noise at 30 dB SNR"},
             "loss": float(loss.sum().item()), "precision": args.precision, "autotune": autotune,
             "accuracy": accuracy,
             "device_status": op.device_status()}
@@ -479,6 +595,20 @@ def run_ours(args):
         line["fp32_comparison"] = {"value": v32, "unit": "applies/s", "ms_per_step": ms32, "steps": args.fp32_steps,
                                    "speedup_bf16x3_over_fp32": value / v32,
                                    "rel_l2_grad_bf16x3_vs_fp32": (accuracy or {}).get("rel_l2_grad_vs_fp32")}
+        if args.precision == "bf16x3-folded":
+            # the element-contraction split-BF16 path of the same plan (tensor cores over slots and elements)
+            op.set_precision("bf16x3")
+            step()
+            torch.cuda.synchronize()
+            e0.record(torch.cuda.current_stream())
+            for _ in range(args.fp32_steps):
+                step()
+            e1.record(torch.cuda.current_stream())
+            torch.cuda.synchronize()
+            mse = e0.elapsed_time(e1) / args.fp32_steps
+            line["bf16x3_element_comparison"] = {"value": world * B / (mse / 1e3), "unit": "applies/s",
+                                                 "ms_per_step": mse, "steps": args.fp32_steps,
+                                                 "speedup_folded_over_element": value / (world * B / (mse / 1e3))}
         op.set_precision(args.precision)  # the timings below use the bench's own path again
     # received energies ||Phi e_p||^2 of the same plan (energy_rx, once per operator in the reference's solvers)
     op.energy_rx()
@@ -502,8 +632,7 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     op.close()
-    if world > 1:
-        dist.destroy_process_group()
+    replicas_end(dist)
 
 
 def run_lasso(args):
@@ -519,9 +648,7 @@ def run_lasso(args):
     import torch
 
     world, rank, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = replicas_begin(world)
     torch.cuda.set_device(local)
     from comp_ui_toolbox_gb300 import OperatorBorn, launch_count
     from comp_ui_toolbox_gb300.workloads import lasso_batch, plan_bytes_estimate
@@ -590,9 +717,13 @@ def run_lasso(args):
     graph = capture(precision)
     n_launch_graph = launch_count() - n_launch_graph
     with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        replicas_barrier(dist)
         clocks.mark_start()
         ms, _ = timed(graph, args.steps, args.warmup)
         clocks.mark_end()
+    replicas_barrier(dist)
+    ms = replicas_max_ms(dist, ms, device="cuda")
     objective = []
     for op, g, u, lam in zip(ops, gs, us, lams):
         r = op.forward(g.t().contiguous()) - u.t()
@@ -647,14 +778,15 @@ def run_lasso(args):
         print(json.dumps(line), flush=True)
     for op in ops:
         op.close()
-    if world > 1:
-        dist.destroy_process_group()
+    replicas_end(dist)
 
 
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_as_replicas(args.gpus))
     if args.precision is None:
-        args.precision = {"2d-batched": "bf16x3", "3d": "fp32"}.get(args.workload, "auto")
+        args.precision = {"2d-batched": "bf16x3-folded", "3d": "fp32"}.get(args.workload, "auto")
     if args.table_storage is None:
         args.table_storage = {"3d": "streamed"}.get(args.workload, "auto")
     if args.impl == "reference":

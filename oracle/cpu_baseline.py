@@ -120,9 +120,12 @@ def time_sample(name: str = "c1", n_waves: int = 1, n_freq: int = 8, processes: 
             if check and r == 0:
                 outs = res
     t_sample = min(times)
-    t_full = t_sample * (S_full / S_sample) * (n_mix_full / n_mix) * (P_full / P_sample)
+    scale = (S_full / S_sample) * (n_mix_full / n_mix) * (P_full / P_sample)
+    t_full = t_sample * scale
     result = {
         "seconds_sample": t_sample,
+        "seconds_per_repeat": times,
+        "scale": scale,
         "seconds_full_apply": t_full,
         "applies_per_s": n_objects / t_full,  # object-applies: all columns go through one BLAS call per element
         "cores": procs,
