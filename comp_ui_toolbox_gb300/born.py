@@ -138,6 +138,7 @@ _SIGNATURES = {
     "cui_born_lasso_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
                                       C.c_void_p, C.c_float, C.c_int32]),
     "cui_born_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64]),
+    "cui_born_set_occupancy_limit": (C.c_int, [C.c_void_p, C.c_int64]),
     "cui_born_energy_rx": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "cui_born_omp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int64), C.c_void_p,
                                C.POINTER(C.c_float), C.POINTER(C.c_int32), C.c_void_p]),
@@ -396,6 +397,11 @@ class OperatorBorn:
     def set_wait_limit(self, nanoseconds: int = 0) -> None:
         """Wall-clock limit of the tensor-core kernels' waits (``cui_born_set_wait_limit``; 0: 1 s)."""
         _check(self._lib.cui_born_set_wait_limit(self._plan, int(nanoseconds)))
+
+    def set_occupancy_limit(self, max_points: int = -1) -> None:
+        """FP32 forward: contract over the occupied points when there are at most ``max_points``
+        (``cui_born_set_occupancy_limit``; -1: N_points / 16, 0: always dense)."""
+        _check(self._lib.cui_born_set_occupancy_limit(self._plan, int(max_points)))
 
     def device_status(self) -> int:
         """Read and clear the device status word (raises CuiError on a timed-out wait)."""

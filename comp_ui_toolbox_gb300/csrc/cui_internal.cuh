@@ -97,6 +97,11 @@ struct Plan {
     float2* ws_G = nullptr;         // [S][B][E] element signals / unmixed data
     float2* ws_r = nullptr;         // [B][n_obs] residual of the VJP
     float* ws_loss = nullptr;       // [B] loss partial sums
+    // occupancy compaction of the FP32 forward (points where any column of gamma is nonzero)
+    int* occ_idx = nullptr;         // [P] occupied points, ascending
+    int* occ_cnt = nullptr;         // [2 * occ_nblk + 2]: per-block counts, offsets, then n_occ and the choice
+    int occ_nblk = 0;               // 1024-point blocks
+    int64_t occ_limit = -1;         // compact when n_occ <= occ_limit (-1: P / 16; 0: never)
 
     // launch geometry chosen at creation
     int fwd_groups = 1;             // line groups of the dense forward

@@ -113,10 +113,12 @@ struct FwdArgs {
     int eyb, n_eyb;             // element rows (ey) per block, blocks per line group
     int B, npass;
     float2* __restrict__ part;  // [groups][S][B][E]
+    const int* occ_sel;         // non-null: the occupancy pass's choice; 1 = the compacted forward runs instead
 };
 
 template <int NC, int KE, bool GEN>
 __device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
+    if (a.occ_sel && *a.occ_sel != 0) return;  // uniform over the block
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
     const int EB = a.eyb;
@@ -262,8 +264,10 @@ __global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_dense3_kernel(const Fw
     fwd_dense_body<NC, KE, false>(a);
 }
 
-// G[s][b][e] = sum over line groups of the forward partials
-__global__ void reduce_groups_kernel(const float2* __restrict__ part, int groups, int64_t n, float2* __restrict__ G) {
+// G[s][b][e] = sum over line groups of the forward partials (skipped when the compacted forward ran)
+__global__ void reduce_groups_kernel(const float2* __restrict__ part, int groups, int64_t n, float2* __restrict__ G,
+                                     const int* occ_sel = nullptr) {
+    if (occ_sel && *occ_sel != 0) return;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         float2 s = make_float2(0.f, 0.f);
@@ -847,7 +851,7 @@ cudaError_t stream_table_chunk(const Plan* p, int f0, int nf, cudaStream_t st) {
 }
 
 template <int NC, int KE>
-cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
+cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, const int* occ_sel) {
     const FwdShape sh = fwd_shape(p, KE);
     FwdArgs a;
     a.g = geom_of(p);
@@ -859,6 +863,7 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
     a.eyb = fwd_rows_per_block(p->Ey); a.n_eyb = (p->Ey + a.eyb - 1) / a.eyb;
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = p->ws_part;
+    a.occ_sel = occ_sel;
     const size_t smem = fwd_smem_bytes(p, NC);
     void (*kern)(const FwdArgs) = p->table_mode == CUI_STORAGE_GENERATED ? fwd_gen_kernel<NC, KE>
                                   : p->n_dims == 3 || NC * KE >= 16       ? fwd_dense3_kernel<NC, KE>
@@ -926,9 +931,9 @@ cudaError_t launch_adj_k(const Plan* p, int B, cudaStream_t st) {
 constexpr int fwd_window(int nc, int ex) { return (ex < 32 * fwd_ke(nc) && fwd_ke(nc) > 2) ? 2 : fwd_ke(nc); }
 
 template <int NC>
-cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st) {
-    if (fwd_window(NC, p->Ex) == 2) return launch_fwd_k<NC, 2>(p, gamma, ldg, B, st);
-    return launch_fwd_k<NC, fwd_ke(NC)>(p, gamma, ldg, B, st);
+cudaError_t launch_fwd(const Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, const int* occ_sel) {
+    if (fwd_window(NC, p->Ex) == 2) return launch_fwd_k<NC, 2>(p, gamma, ldg, B, st, occ_sel);
+    return launch_fwd_k<NC, fwd_ke(NC)>(p, gamma, ldg, B, st, occ_sel);
 }
 
 template <int NC>
@@ -945,6 +950,174 @@ cudaError_t launch_adj(const Plan* p, int B, cudaStream_t st) {
 int grid_1d(int64_t n, int threads) {
     const int64_t b = (n + threads - 1) / threads;
     return static_cast<int>(std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32));
+}
+
+// ---------------------------------------------------------------------------
+// occupancy compaction (FP32 forward): the reference's forward contracts only the grid points
+// where some column of gamma is nonzero (operator_born.m:361, combined_quick_gpu.cu:457-499).
+// A count / scan / scatter pass lists those points in ascending order and chooses, on the
+// device, the compacted forward when they are few (n_occ <= limit) and the dense kernels
+// otherwise; the kernel not chosen returns at once, so the choice needs no host round trip.
+// ---------------------------------------------------------------------------
+constexpr int kOccBlock = 1024;  // points per block of the count and scatter kernels (one per thread)
+
+__device__ __forceinline__ bool occupied(const float2* __restrict__ g, int64_t ldg, int B, int64_t pt) {
+    for (int b = 0; b < B; ++b) {
+        const float2 v = g[static_cast<int64_t>(b) * ldg + pt];
+        if (v.x != 0.f || v.y != 0.f) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kOccBlock) occ_count_kernel(const float2* __restrict__ g, int64_t ldg, int B,
+                                                              int64_t P, int* __restrict__ cnt) {
+    const int64_t pt = static_cast<int64_t>(blockIdx.x) * kOccBlock + threadIdx.x;
+    const int n = __syncthreads_count(pt < P && occupied(g, ldg, B, pt));
+    if (threadIdx.x == 0) cnt[blockIdx.x] = n;
+}
+
+// one block: exclusive scan of the block counts into offsets; n_occ and the choice after them
+__global__ void __launch_bounds__(1024) occ_scan_kernel(int* __restrict__ cnt, int nblk, int64_t limit) {
+    __shared__ int warp_sum[32];
+    const int tid = threadIdx.x, per = (nblk + 1023) / 1024;
+    const int lo = min(nblk, tid * per), hi = min(nblk, lo + per);
+    int mine = 0;
+    for (int i = lo; i < hi; ++i) mine += cnt[i];
+    // inclusive scan of the per-thread sums: warps, then the warp totals
+    int v = mine;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, v, d);
+        if ((tid & 31) >= d) v += o;
+    }
+    if ((tid & 31) == 31) warp_sum[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        int w = warp_sum[tid];
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, w, d);
+            if (tid >= d) w += o;
+        }
+        warp_sum[tid] = w;
+    }
+    __syncthreads();
+    int run = v - mine + ((tid >> 5) ? warp_sum[(tid >> 5) - 1] : 0);  // exclusive prefix of this thread
+    for (int i = lo; i < hi; ++i) {
+        const int c = cnt[i];
+        cnt[nblk + i] = run;
+        run += c;
+    }
+    if (tid == 1023) {
+        const int total = warp_sum[31];
+        cnt[2 * nblk] = total;
+        cnt[2 * nblk + 1] = (limit > 0 && total <= limit) ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(kOccBlock) occ_scatter_kernel(const float2* __restrict__ g, int64_t ldg, int B,
+                                                                int64_t P, const int* __restrict__ cnt, int nblk,
+                                                                int* __restrict__ idx) {
+    if (cnt[2 * nblk + 1] == 0) return;  // the dense kernels run: no list needed
+    __shared__ int warp_cnt[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t pt = static_cast<int64_t>(blockIdx.x) * kOccBlock + tid;
+    const bool occ = pt < P && occupied(g, ldg, B, pt);
+    const unsigned ballot = __ballot_sync(0xffffffffu, occ);
+    if (lane == 0) warp_cnt[w] = __popc(ballot);
+    __syncthreads();
+    int before = 0;
+    for (int k = 0; k < w; ++k) before += warp_cnt[k];
+    if (occ) idx[cnt[nblk + blockIdx.x] + before + __popc(ballot & ((1u << lane) - 1u))] = static_cast<int>(pt);
+}
+
+struct SparseFwdArgs {
+    LineGeom g;
+    const float2* __restrict__ table;  // stored table, or null: entries generated (gen)
+    TableGen gen;
+    const float2* __restrict__ p_in;
+    const float2* __restrict__ gamma;
+    int64_t ldg;
+    const int* __restrict__ slot_f;
+    const int* __restrict__ idx;
+    const int* __restrict__ cnt;       // n_occ at [2 nblk], the choice at [2 nblk + 1]
+    int nblk, B;
+    float2* __restrict__ G;            // [S][B][E]
+};
+
+constexpr int kSpThreads = 256;
+constexpr int kSpMaxPerThread = 4;  // elements per thread: arrays of up to 1024 elements
+
+// G[s][b][e] = sum over the occupied points p of h(f_s; o(p, e), z_p) p_in[s][p] gamma[b][p]:
+// block per (slot, object), thread per element (up to 4), the points staged 256 at a time with
+// their q = p_in gamma and grid coordinates
+template <bool GEN>
+__global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdArgs a) {
+    if (a.cnt[2 * a.nblk + 1] == 0) return;  // the dense kernels run instead
+    const LineGeom& g = a.g;
+    const int s = blockIdx.x, b = blockIdx.y, f = a.slot_f[s];
+    const int n_occ = a.cnt[2 * a.nblk];
+    __shared__ float2 sq[kSpThreads];
+    __shared__ int sx[kSpThreads], sy[kSpThreads], sz[kSpThreads];
+    float2 acc[kSpMaxPerThread];
+#pragma unroll
+    for (int k = 0; k < kSpMaxPerThread; ++k) acc[k] = make_float2(0.f, 0.f);
+    const float2* pin = a.p_in + static_cast<int64_t>(s) * g.P;
+    const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg;
+    for (int t0 = 0; t0 < n_occ; t0 += kSpThreads) {
+        const int j = t0 + threadIdx.x;
+        if (j < n_occ) {
+            const int pt = a.idx[j];
+            sq[threadIdx.x] = cmul(pin[pt], gam[pt]);
+            const int x = pt % g.Nx, rest = pt / g.Nx;
+            sx[threadIdx.x] = x;
+            sy[threadIdx.x] = rest % g.Ny;
+            sz[threadIdx.x] = rest / g.Ny;
+        }
+        __syncthreads();
+        const int nt = min(kSpThreads, n_occ - t0);
+        for (int k = 0; k < kSpMaxPerThread; ++k) {
+            const int e = threadIdx.x + k * kSpThreads;
+            if (e >= g.E) break;
+            const int ey = e / g.Ex, ex = e - ey * g.Ex;
+            for (int i = 0; i < nt; ++i) {
+                const int ox = sx[i] + (g.Ex - 1 - ex) * g.ppx, oy = sy[i] + (g.Ey - 1 - ey) * g.ppy;
+                float2 h;
+                if constexpr (GEN)
+                    h = gen_entry(a.gen, gen_row(a.gen, f, sz[i], oy), ox);
+                else
+                    h = __ldg(a.table + ((static_cast<int64_t>(f) * g.Nz + sz[i]) * g.Noy + oy) * g.Nox + ox);
+                cmac(acc[k], h, sq[i]);
+            }
+        }
+        __syncthreads();
+    }
+    for (int k = 0; k < kSpMaxPerThread; ++k) {
+        const int e = threadIdx.x + k * kSpThreads;
+        if (e < g.E) a.G[(static_cast<int64_t>(s) * a.B + b) * g.E + e] = acc[k];
+    }
+}
+
+// the occupancy pass and the compacted forward; returns the choice word the dense kernels read
+cudaError_t launch_occupancy(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, const int** sel) {
+    *sel = nullptr;
+    if (!p->occ_idx || p->E > kSpThreads * kSpMaxPerThread) return cudaSuccess;
+    const int64_t limit = p->occ_limit < 0 ? p->P / 16 : p->occ_limit;
+    if (limit == 0) return cudaSuccess;
+    occ_count_kernel<<<p->occ_nblk, kOccBlock, 0, st>>>(gamma, ldg, B, p->P, p->occ_cnt);
+    occ_scan_kernel<<<1, 1024, 0, st>>>(p->occ_cnt, p->occ_nblk, limit);
+    occ_scatter_kernel<<<p->occ_nblk, kOccBlock, 0, st>>>(gamma, ldg, B, p->P, p->occ_cnt, p->occ_nblk, p->occ_idx);
+    SparseFwdArgs a;
+    a.g = geom_of(p);
+    a.table = p->table; a.gen = p->gen; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
+    a.slot_f = p->slot_f; a.idx = p->occ_idx; a.cnt = p->occ_cnt; a.nblk = p->occ_nblk; a.B = B; a.G = p->ws_G;
+    // entries are generated where the table is not stored (the chunk buffer of a streamed plan is
+    // refilled by the dense launch)
+    if (p->table_mode == CUI_STORAGE_STORED)
+        sparse_fwd_kernel<false><<<dim3(p->S, B), kSpThreads, 0, st>>>(a);
+    else
+        sparse_fwd_kernel<true><<<dim3(p->S, B), kSpThreads, 0, st>>>(a);
+    count_launch(4);
+    *sel = p->occ_cnt + 2 * p->occ_nblk + 1;
+    return cudaGetLastError();
 }
 
 // forward against the folded operator: 64-object GEMM passes, each reduced over its K chunks into u
@@ -966,22 +1139,26 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     cudaError_t e;
     if (p->precision == 2) return run_forward_phi(p, gamma, ldg, B, u, ldu, st);
     int groups = p->fwd_groups;
+    const int* occ_sel = nullptr;
     if (p->precision == 1 && p->tc2) {
         e = launch_fwd_tc2(p, gamma, ldg, B, st, &groups);
     } else if (p->precision == 1) {
         e = launch_fwd_tc(p, gamma, ldg, B, st);
-    } else switch (pick_nc(p->max_slots_per_f)) {
-        case 1: e = launch_fwd<1>(p, gamma, ldg, B, st); break;
-        case 2: e = launch_fwd<2>(p, gamma, ldg, B, st); break;
-        case 4: e = launch_fwd<4>(p, gamma, ldg, B, st); break;
-        case 6: e = launch_fwd<6>(p, gamma, ldg, B, st); break;
-        case 8: e = launch_fwd<8>(p, gamma, ldg, B, st); break;
-        case 12: e = launch_fwd<12>(p, gamma, ldg, B, st); break;
-        default: e = launch_fwd<16>(p, gamma, ldg, B, st); break;
+    } else {
+        if ((e = launch_occupancy(p, gamma, ldg, B, st, &occ_sel)) != cudaSuccess) return e;
+        switch (pick_nc(p->max_slots_per_f)) {
+            case 1: e = launch_fwd<1>(p, gamma, ldg, B, st, occ_sel); break;
+            case 2: e = launch_fwd<2>(p, gamma, ldg, B, st, occ_sel); break;
+            case 4: e = launch_fwd<4>(p, gamma, ldg, B, st, occ_sel); break;
+            case 6: e = launch_fwd<6>(p, gamma, ldg, B, st, occ_sel); break;
+            case 8: e = launch_fwd<8>(p, gamma, ldg, B, st, occ_sel); break;
+            case 12: e = launch_fwd<12>(p, gamma, ldg, B, st, occ_sel); break;
+            default: e = launch_fwd<16>(p, gamma, ldg, B, st, occ_sel); break;
+        }
     }
     if (e != cudaSuccess) return e;
     const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
-    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G);
+    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G, occ_sel);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (use_mix_tile(p, B)) {
@@ -1236,6 +1413,7 @@ cudaError_t launch_fwd_static_k(const Plan* p, const float2* gamma, int64_t ldg,
     a.eyb = fwd_rows_per_block(p->Ey); a.n_eyb = (p->Ey + a.eyb - 1) / a.eyb;
     a.B = B; a.npass = (p->max_slots_per_f + NC - 1) / NC;
     a.part = part;
+    a.occ_sel = nullptr;
     const size_t smem = fwd_smem_bytes(p, NC);
     // a table that is not stored (generated or streamed) is generated inside the kernel here: the
     // chunk buffer of a streamed plan may be in use by work on another stream

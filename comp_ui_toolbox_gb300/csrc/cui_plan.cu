@@ -489,6 +489,9 @@ cui_status upload_metadata_and_workspace(Plan& p) {
     CUI_TRY(dalloc(p, &p.ws_G, static_cast<size_t>(p.S) * B * p.E));
     CUI_TRY(dalloc(p, &p.ws_r, static_cast<size_t>(p.n_obs) * B));
     CUI_TRY(dalloc(p, &p.ws_loss, loss_workspace_floats(B)));
+    p.occ_nblk = static_cast<int>((p.P + 1023) / 1024);
+    CUI_TRY(dalloc(p, &p.occ_idx, static_cast<size_t>(p.P)));
+    CUI_TRY(dalloc(p, &p.occ_cnt, static_cast<size_t>(2 * p.occ_nblk + 2)));
     p.workspace_bytes = p.ws_part_bytes +
                         sizeof(float2) * (static_cast<size_t>(p.S) * B * p.E + static_cast<size_t>(p.n_obs) * B) +
                         sizeof(float) * loss_workspace_floats(B);

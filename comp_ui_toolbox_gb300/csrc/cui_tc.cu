@@ -623,6 +623,14 @@ extern "C" cui_status cui_born_set_wait_limit(cui_born_plan* plan, int64_t nanos
     return CUI_OK;
 }
 
+extern "C" cui_status cui_born_set_occupancy_limit(cui_born_plan* plan, int64_t max_points) {
+    using namespace cui;
+    if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
+    if (max_points < -1) return set_error(CUI_ERR_INVALID_ARG, "max_points must be -1 (default), 0 (off) or > 0");
+    plan->p.occ_limit = max_points;
+    return CUI_OK;
+}
+
 extern "C" cui_status cui_born_plan_status(cui_born_plan* plan, int32_t* device_status) {
     using namespace cui;
     if (!plan || !device_status) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");

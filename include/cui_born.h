@@ -441,6 +441,14 @@ cui_status cui_born_timing_enable(cui_born_plan* plan, int32_t enable);
  * their work until the status is read.  nanoseconds = 0 restores the default of
  * 1 s; otherwise 1 ns to 60 s. */
 cui_status cui_born_set_wait_limit(cui_born_plan* plan, int64_t nanoseconds);
+/* Occupancy compaction of the FP32 forward (operator_born.m:361, combined_quick_gpu.cu:457-499:
+ * the reference contracts only the grid points where some column of gamma is nonzero).  Every
+ * FP32 forward first lists those points on the device; when there are at most max_points of
+ * them it contracts over the list (work proportional to their number), otherwise it runs the
+ * dense kernels.  The choice is made on the device (no synchronisation).  max_points = -1
+ * selects the default, N_points / 16; 0 turns the compaction off.  The split-BF16 paths
+ * always contract densely. */
+cui_status cui_born_set_occupancy_limit(cui_born_plan* plan, int64_t max_points);
 /* Reads and clears the plan's device status word; CUI_ERR_TIMEOUT when a
  * bounded device-side wait gave up since the last call. */
 cui_status cui_born_plan_status(cui_born_plan* plan, int32_t* device_status);
