@@ -220,6 +220,7 @@ cui_status select_device_and_shapes(Plan& p, int device);
 cui_status upload_metadata_and_workspace(Plan& p);
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes);
 // fault injection of device allocations (CUI_BORN_FAIL_ALLOC=N: the plan's N-th allocation fails)
+void release_since(Plan& p, size_t mark);  // frees the plan's allocations made since index `mark`
 bool injected_alloc_failure(Plan& p);
 // table cache (cui_cache.cu): canonical key of the setup fields the device tables depend on,
 // its file path under `dir` (the incident fields alone when the table is not stored), and

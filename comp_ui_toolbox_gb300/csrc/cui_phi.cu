@@ -421,12 +421,6 @@ cui_status copy_back(std::vector<T>& h, const T* d, size_t n) {
     return check_cuda(cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost), "folded operator metadata");
 }
 
-// frees the plan's allocations made since index `mark` (a failed build leaves nothing behind)
-void release_since(Plan& p, size_t mark) {
-    for (size_t i = mark; i < p.allocations.size(); ++i) cudaFree(p.allocations[i]);
-    p.allocations.resize(std::min(mark, p.allocations.size()));
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------

@@ -25,6 +25,7 @@ size_t loss_workspace_floats(int max_objects);
 
 namespace {
 thread_local std::string g_last_error;
+thread_local int g_injected = 0;  // number of the allocation that the injector failed last, not yet reported
 std::atomic<int64_t> g_launches{0};
 constexpr size_t kPartBudget = size_t(1) << 30;  // bytes of partial-sum scratch a plan may hold
 }  // namespace
@@ -36,7 +37,12 @@ cui_status set_error(cui_status s, const std::string& msg) {
 
 cui_status check_cuda(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return CUI_OK;
-    if (e == cudaErrorMemoryAllocation) return set_error(CUI_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) {
+        std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+        if (g_injected) msg += " (injected allocation failure " + std::to_string(g_injected) + ", CUI_BORN_FAIL_ALLOC)";
+        g_injected = 0;
+        return set_error(CUI_ERR_OOM, msg);
+    }
     return set_error(CUI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
@@ -48,7 +54,9 @@ void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool injected_alloc_failure(Plan& p) {
     const char* env = std::getenv("CUI_BORN_FAIL_ALLOC");
     ++p.n_device_allocs;
-    return env && env[0] && std::atoi(env) == p.n_device_allocs;
+    const bool fail = env && env[0] && std::atoi(env) == p.n_device_allocs;
+    if (fail) g_injected = p.n_device_allocs;
+    return fail;
 }
 
 namespace {
@@ -498,10 +506,14 @@ cui_status upload_metadata_and_workspace(Plan& p) {
     return CUI_OK;
 }
 
+// frees the plan's allocations made since index `mark` (a failed build leaves nothing behind)
+void release_since(Plan& p, size_t mark) {
+    for (size_t i = mark; i < p.allocations.size(); ++i) cudaFree(p.allocations[i]);
+    p.allocations.resize(std::min(mark, p.allocations.size()));
+}
+
 cui_status device_alloc(Plan& p, void** ptr, size_t bytes) {
-    if (injected_alloc_failure(p))
-        return set_error(CUI_ERR_OOM, "cudaMalloc: injected allocation failure " + std::to_string(p.n_device_allocs) +
-                                          " (CUI_BORN_FAIL_ALLOC)");
+    if (injected_alloc_failure(p)) return check_cuda(cudaErrorMemoryAllocation, "cudaMalloc");
     void* v = nullptr;
     cudaError_t e = cudaMalloc(&v, std::max<size_t>(bytes, 1));
     if (e != cudaSuccess) return check_cuda(e, "cudaMalloc");

@@ -546,10 +546,7 @@ bool tc_supported(const Plan* p, std::string* why) {
     return true;
 }
 
-cui_status tc_prepare(Plan& p) {
-    std::string why;
-    if (!tc_supported(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
-    if (p.tb) return CUI_OK;
+cui_status tc_build(Plan& p) {
     p.Epad = (p.Ex + 7) / 8 * 8;
     p.Jpad = 8;
     while (p.Jpad < p.Nj_max) p.Jpad *= 2;  // power of two <= 128: one point per thread for every column
@@ -557,11 +554,6 @@ cui_status tc_prepare(Plan& p) {
     p.tb_vstride = static_cast<int64_t>(p.F) * p.Nz * p.Noy * p.ppx * p.Nb;
     cui_status st = device_alloc(p, reinterpret_cast<void**>(&p.tb), sizeof(uint32_t) * 2 * p.tb_vstride);
     if (st != CUI_OK) return st;
-    if (!p.ws_status) {
-        if ((st = device_alloc(p, reinterpret_cast<void**>(&p.ws_status), sizeof(int))) != CUI_OK) return st;
-        cudaError_t e = cudaMemset(p.ws_status, 0, sizeof(int));
-        if (e != cudaSuccess) return check_cuda(e, "cudaMemset");
-    }
     int smem_optin = 0;
     cudaError_t e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device);
     if (e != cudaSuccess) return check_cuda(e, "cudaDeviceGetAttribute");
@@ -577,6 +569,27 @@ cui_status tc_prepare(Plan& p) {
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return check_cuda(e, "band table");
     p.tc_bytes = sizeof(uint32_t) * 2 * static_cast<size_t>(p.tb_vstride);
     return CUI_OK;
+}
+
+// Residue-unit split tables, built once; a build that fails frees what it allocated and leaves the
+// plan as it was (the next switch starts over).
+cui_status tc_prepare(Plan& p) {
+    std::string why;
+    if (!tc_supported(&p, &why)) return set_error(CUI_ERR_UNSUPPORTED_SETUP, why);
+    if (p.tb) return CUI_OK;
+    if (!p.ws_status) {
+        cui_status st = device_alloc(p, reinterpret_cast<void**>(&p.ws_status), sizeof(int));
+        if (st != CUI_OK) return st;
+        cudaError_t e = cudaMemset(p.ws_status, 0, sizeof(int));
+        if (e != cudaSuccess) return check_cuda(e, "cudaMemset");
+    }
+    const size_t mark = p.allocations.size();
+    const cui_status s = tc_build(p);
+    if (s != CUI_OK) {
+        release_since(p, mark);
+        p.tb = nullptr;
+    }
+    return s;
 }
 
 

@@ -139,23 +139,32 @@ __device__ __forceinline__ bool bar_try_wait_hint(uint32_t bar, uint32_t parity,
     return ok != 0;
 }
 
+// non-blocking test of the phase with the given parity
+__device__ __forceinline__ bool bar_test_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Wait with a wall-clock limit shared by the whole block: gives up (and raises
-// *abort for everyone else) after `limit_ns`, or as soon as another thread of
-// the block has given up.
+// *abort for everyone else) once `limit_ns` have passed since the call, or as soon as
+// another thread of the block has given up.  A phase that is already complete costs
+// one test and no clock read; after that the clock and the flag are read after every
+// suspended poll, so that a limit shorter than one poll runs out at the first one.
 __device__ __forceinline__ bool bar_wait_abortable(uint32_t bar, uint32_t parity, volatile int* abort,
                                                    uint64_t limit_ns) {
-    uint64_t t0 = 0;
-    for (uint32_t i = 0;; ++i) {
+    if (bar_test_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
         if (bar_try_wait_hint(bar, parity, 2000u)) return true;
-        if ((i & 3u) == 3u) {
-            if (*abort) return false;
-            const uint64_t t = globaltimer_ns();
-            if (t0 == 0) {
-                t0 = t;
-            } else if (t - t0 > limit_ns) {
-                *abort = 1;
-                return false;
-            }
+        if (*abort) return false;
+        if (globaltimer_ns() - t0 > limit_ns) {
+            *abort = 1;
+            return false;
         }
     }
 }

@@ -1142,8 +1142,7 @@ bool tc2_supported(const Plan* p, std::string* why) {
     return true;
 }
 
-cui_status tc2_prepare(Plan& p) {
-    if (p.tr) return CUI_OK;
+cui_status tc2_build(Plan& p) {
     p.Epad = (p.Ex + 15) / 16 * 16;
     p.RowW = (p.Nox + 3) / 4 * 4;
     p.Jp = ((p.Nx + 3) / 4 + 1) / 2 * 2;  // points per residue, even: 16-byte rows
@@ -1180,6 +1179,24 @@ cui_status tc2_prepare(Plan& p) {
                   sizeof(float2) * p.P * p.max_objects + vs_bytes;
     p.tc2 = 1;
     return CUI_OK;
+}
+
+// Line-unit tables, built once; a build that fails frees what it allocated and leaves the plan as
+// it was (the next switch starts over).
+cui_status tc2_prepare(Plan& p) {
+    if (p.tc2) return CUI_OK;
+    const size_t mark = p.allocations.size();
+    const size_t tc_bytes0 = p.tc_bytes;
+    const cui_status s = tc2_build(p);
+    if (s != CUI_OK) {
+        release_since(p, mark);
+        p.tr = nullptr;
+        p.p_fw = p.p_ad = nullptr;
+        p.ws_galign = nullptr;
+        p.ws_vs = nullptr;
+        p.tc_bytes = tc_bytes0;
+    }
+    return s;
 }
 
 cudaError_t launch_fwd_tc2(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* groups) {

@@ -27,9 +27,13 @@ def _free():
 def test_every_failed_allocation_of_plan_creation_is_clean(form, monkeypatch):
     from comp_ui_toolbox_gb300 import CuiError, OperatorBorn
     b = configs.build(configs.small_config("c2"))
-    create = (lambda: make_operator(b, "lateral", max_objects=4)) if form == "table" else \
-        (lambda: OperatorBorn.from_setup(**setup_kwargs(b.cfg), device=0, max_objects=4))
-    create().close()  # warm: first-use allocations of the runtime are outside the measurement
+    create = (lambda: make_operator(b, "lateral", max_objects=b.cfg.n_objects)) if form == "table" else \
+        (lambda: OperatorBorn.from_setup(**setup_kwargs(b.cfg), device=0, max_objects=b.cfg.n_objects))
+    gamma = configs.make_gamma(b.cfg)
+    g = torch.from_numpy(gamma.astype(np.complex64)).cuda()
+    op = create()  # warm: first-use loads of kernel modules (the library's and torch's) are outside the measurement
+    op.forward(g).cpu()
+    op.close()
     free0 = _free()
     n = 1
     while n < 200:
@@ -45,8 +49,7 @@ def test_every_failed_allocation_of_plan_creation_is_clean(form, monkeypatch):
         break
     monkeypatch.delenv("CUI_BORN_FAIL_ALLOC")
     assert n > 5  # several allocations were failed one at a time
-    gamma = configs.make_gamma(b.cfg)
-    u = op.forward(torch.from_numpy(gamma.astype(np.complex64)).cuda()).cpu().numpy()
+    u = op.forward(g).cpu().numpy()
     assert rel_l2(u, forward_quick_cpu(b.op, gamma)) <= 1e-5
     op.close()
     assert abs(_free() - free0) <= SLACK
@@ -57,7 +60,7 @@ def test_failed_precision_switch_keeps_the_plan_working(precision, monkeypatch):
     """Fail the j-th allocation of the switch for j = 1, 2, ... until it succeeds."""
     from comp_ui_toolbox_gb300 import CuiError
     b = configs.build(configs.small_config("c2"))
-    op = make_operator(b, "lateral", max_objects=4)
+    op = make_operator(b, "lateral", max_objects=b.cfg.n_objects)
     gamma = configs.make_gamma(b.cfg)
     g = torch.from_numpy(gamma.astype(np.complex64)).cuda()
     u_ref = forward_quick_cpu(b.op, gamma)

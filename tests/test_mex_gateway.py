@@ -166,7 +166,7 @@ def test_lasso_mex_matches_device_lasso(lasso_mex):
     g_mex = lasso_mex.call_args([node, d(u), d(np.array(lam)), d(np.array(step)), d(np.array(20.0)),
                                  d(np.zeros((b.op.setup.n_points, 1), dtype=complex))])
     assert np.abs(g_mex).max() > 0
-    assert rel_l2(g_mex[:, 0], g_dev.cpu().numpy()) <= 1e-4
+    assert rel_l2(g_mex[:, 0], g_dev.cpu().numpy().reshape(-1)) <= 1e-4
     op.close()
     lasso_mex.reset()
     lasso_mex.lib.ref_clear_mex()
