@@ -63,8 +63,10 @@ def parse():
                          "3d, whose configuration recomputes the table; auto otherwise)")
     ap.add_argument("--lasso-streams", type=int, default=4,
                     help="2d-lasso: concurrent streams the problems are spread over inside the graph")
-    ap.add_argument("--lasso-problems", type=int, default=16,
-                    help="2d-lasso: how many of the 256 seeded problems go into the graph (device memory bound)")
+    ap.add_argument("--lasso-problems", type=int, default=256,
+                    help="2d-lasso: how many of the seeded uneven problems the job holds (the configuration's 256)")
+    ap.add_argument("--lasso-budget-gb", type=float, default=None,
+                    help="2d-lasso: device memory the plans of one batch may hold (default: 85 %% of free memory)")
     ap.add_argument("--lasso-iters", type=int, default=50)
     ap.add_argument("--n-freq", type=int, default=None,
                     help="keep only the first N frequencies (reduced case for profiler captures)")
@@ -637,14 +639,43 @@ def run_ours(args):
     replicas_end(dist)
 
 
-def run_lasso(args):
-    """Uneven-batch solver loop: every problem's LASSO iterations captured into one CUDA graph.
+LASSO_CHECK_PROBLEM = 230  # the problem of the 256 with the least work: the CPU sample and the FP64 check
 
-    One step = one replay of the graph = ``--lasso-iters`` proximal-gradient
-    iterations (forward, residual, adjoint, soft threshold) of each of the
-    first ``--lasso-problems`` problems of the seeded batch; the problems run
-    concurrently on ``--lasso-streams`` streams inside the graph.  ``value`` counts one
-    forward + adjoint apply per problem per iteration.
+
+def lasso_macs(w) -> int:
+    """Complex multiply-adds of one forward apply of a problem of the uneven batch (no receive
+    mixing: every slot contracts all elements over all points)."""
+    return len(w.f) * len(w.waves) * w.n_elements * w.n_points
+
+
+def run_lasso(args):
+    """Uneven-batch solver loop: all seeded problems (default 256), ``--lasso-iters``
+    proximal-gradient LASSO iterations each (forward, residual, adjoint, soft threshold).
+
+    The problems' plans need more device memory together than one GPU holds (about 956 GB
+    with the split-BF16 copies, 322 GB in FP32).  So they run in batches that fit a
+    device-memory budget.  For each batch, in seeded order:
+
+    - the batch's plans are built;
+    - the iterations of all its problems are captured into one CUDA graph, the problems spread
+      over ``--lasso-streams`` streams;
+    - the graph is replayed once;
+    - the solutions are read back and the plans freed before the next batch.
+
+    A preparation pass comes first.  It is untimed, and it also runs every kernel of every
+    problem.  For each problem it:
+
+    - builds the plan once and synthesises the data on the device: u = Phi gamma_true + 25 dB
+      noise, lambda = 0.05 ||Phi^H u||_inf, step = 0.9 / ||Phi||^2 from 8 power iterations;
+    - picks the path, with the per-plan autotuner by default;
+    - measures the plan's device bytes on each path;
+    - keeps u in pinned host memory (FP64).
+
+    One step = one pass over all problems.  ``value`` = problems x iterations / the summed
+    graph-replay time (CUDA events, every plan of the batch resident).  ``e2e`` = the same count
+    / the pass's wall time, with every plan rebuilt, u copied from the host, the graphs captured
+    and replayed, and the solutions copied back.  With several replicas the problems are split
+    over them (they are independent); the job is fixed, so the scaling is strong.
     """
     import numpy as np
     import torch
@@ -653,134 +684,302 @@ def run_lasso(args):
     dist = replicas_begin(world)
     torch.cuda.set_device(local)
     from comp_ui_toolbox_gb300 import OperatorBorn, launch_count
-    from comp_ui_toolbox_gb300.workloads import lasso_batch, plan_bytes_estimate
+    from comp_ui_toolbox_gb300.workloads import lasso_batch
 
     probs = lasso_batch(args.lasso_problems)
+    mine = list(range(rank, len(probs), world))
     n_it = args.lasso_iters
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    budget = int(args.lasso_budget_gb * 1e9) if args.lasso_budget_gb else int(0.85 * free0)
+
+    def used_bytes(reserved0, free_before):
+        torch.cuda.synchronize()
+        return (free_before - torch.cuda.mem_get_info()[0]) - (torch.cuda.memory_reserved() - reserved0)
+
+    # ---- preparation pass (untimed) ----
     t0 = time.perf_counter()
-    ops, us, lams, steps, gs = [], [], [], [], []
-    gen = torch.Generator(device="cuda").manual_seed(11)
-    for w in probs:
+    prep = {}
+    for i in mine:
+        w = probs[i]
+        torch.cuda.synchronize()
+        f_before, r_before = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
         op = OperatorBorn.from_setup(**w.setup_kwargs(), device=local, max_objects=1)
         g_true = torch.from_numpy(w.gamma(n_objects=1).astype(np.complex64)).cuda()
         u = op.forward(g_true)
+        gen = torch.Generator(device="cuda").manual_seed(11 + i)
         noise = torch.randn(u.shape, dtype=torch.complex64, device="cuda", generator=gen)
         u = u + noise * (u.abs().pow(2).mean().sqrt() / noise.abs().pow(2).mean().sqrt()) * 10 ** (-25 / 20)
         L = op.norm_estimate(8)
         lam = 0.05 * float(op.adjoint(u).abs().max())
-        ops.append(op)
-        us.append(u.t().contiguous())
-        lams.append(torch.tensor([lam], dtype=torch.float32, device="cuda"))
-        steps.append(0.9 / L)
-        gs.append(torch.zeros((1, op.n_points), dtype=torch.complex64, device="cuda"))
-    torch.cuda.synchronize()
-    t_build = time.perf_counter() - t0
+        rec = {"lam": lam, "step": 0.9 / L}
+        uc = u.t().contiguous()
+        lam_t = torch.tensor([lam], dtype=torch.float32, device="cuda")
+        gtmp = torch.zeros((1, op.n_points), dtype=torch.complex64, device="cuda")
+        op.lasso_(gtmp, uc, lam_t, rec["step"], 1)  # the FP32 path's workspaces exist before the bytes are read
+        rec["bytes_fp32"] = used_bytes(r_before, f_before)
+        if args.precision == "auto":
+            tu = op.autotune(1)
+            rec.update(precision=tu["precision"], shapes=tu["launch_shapes"])
+        else:
+            op.set_precision(args.precision)
+            rec.update(precision=args.precision, shapes=None)
+        op.lasso_(gtmp, uc, lam_t, rec["step"], 1)
+        rec["bytes"] = used_bytes(r_before, f_before)
+        rec["u_host"] = u.reshape(-1).to(torch.complex128).cpu().pin_memory()
+        op.close()
+        del u, uc, gtmp, noise, g_true
+        prep[i] = rec
+    torch.cuda.empty_cache()
+    t_prep = time.perf_counter() - t0
+
+    def batches(key):
+        out, cur, acc = [], [], 0
+        for i in mine:
+            b = prep[i][key] + (64 << 20)  # + graph and stream bookkeeping
+            if cur and acc + b > budget:
+                out.append(cur)
+                cur, acc = [], 0
+            cur.append(i)
+            acc += b
+        if cur:
+            out.append(cur)
+        return out
+
     streams = [torch.cuda.Stream() for _ in range(max(1, args.lasso_streams))]
 
-    tuned = []
-    if args.precision == "auto":  # per-plan autotuner: the faster path for each problem
-        tuned = [op.autotune(1) for op in ops]
-
-    def capture(precision):
-        for op, tu in zip(ops, tuned or [None] * len(ops)):
-            op.set_precision(tu["precision"] if (precision == "auto" and tu) else precision)
-        for op, g, u, lam, st in zip(ops, gs, us, lams, steps):  # first use outside the capture
-            op.lasso_(g, u, lam, st, 1)
+    def solve_pass(fp32: bool, objective=False):
+        key = "bytes_fp32" if fp32 else "bytes"
+        st = {"build_s": 0.0, "h2d_s": 0.0, "capture_s": 0.0, "solve_ms": 0.0, "d2h_s": 0.0, "kernel_nodes": 0,
+              "batches": [], "h2d_bytes": 0, "d2h_bytes": 0}
+        sols, obj = {}, {}
+        t_obj = 0.0
         torch.cuda.synchronize()
-        graph = torch.cuda.CUDAGraph()
-        cap = torch.cuda.Stream()
-        with torch.cuda.graph(graph, stream=cap):
-            for i, (op, g, u, lam, st) in enumerate(zip(ops, gs, us, lams, steps)):
-                s = streams[i % len(streams)]
-                s.wait_stream(cap)
-                with torch.cuda.stream(s):
-                    op.lasso_(g, u, lam, st, n_it)
-            for s in streams:
-                cap.wait_stream(s)
-        return graph
-
-    def timed(graph, n_steps, warm):
-        for _ in range(warm):
-            graph.replay()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        n0 = launch_count()
-        e0.record()
-        for _ in range(n_steps):
+        t_pass = time.perf_counter()
+        for batch in batches(key):
+            t = time.perf_counter()
+            ops = []
+            for i in batch:
+                op = OperatorBorn.from_setup(**probs[i].setup_kwargs(), device=local, max_objects=1)
+                p = "fp32" if fp32 else prep[i]["precision"]
+                op.set_precision(p)
+                sh = prep[i]["shapes"]
+                if p == "bf16x3" and sh:
+                    op.set_launch_shapes(*[v if isinstance(v, int) else 0
+                                           for v in (sh["narrow_tiles"], sh["fwd_blocks"], sh["adj_blocks"])])
+                ops.append(op)
+            torch.cuda.synchronize()
+            st["build_s"] += time.perf_counter() - t
+            t = time.perf_counter()
+            us = [prep[i]["u_host"].to("cuda", non_blocking=True) for i in batch]
+            us = [u.to(torch.complex64).reshape(1, -1).contiguous() for u in us]
+            torch.cuda.synchronize()
+            st["h2d_s"] += time.perf_counter() - t
+            st["h2d_bytes"] += sum(16 * u.numel() for u in us)
+            t = time.perf_counter()
+            lams = [torch.tensor([prep[i]["lam"]], dtype=torch.float32, device="cuda") for i in batch]
+            gs = [torch.zeros((1, op.n_points), dtype=torch.complex64, device="cuda") for op in ops]
+            for op, g, u, lam, i in zip(ops, gs, us, lams, batch):  # first use outside the capture
+                op.lasso_(g, u, lam, prep[i]["step"], 1)
+            torch.cuda.synchronize()
             for g in gs:
                 g.zero_()
+            n0 = launch_count()
+            graph = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream()
+            with torch.cuda.graph(graph, stream=cap):
+                for k, (op, g, u, lam, i) in enumerate(zip(ops, gs, us, lams, batch)):
+                    s = streams[k % len(streams)]
+                    s.wait_stream(cap)
+                    with torch.cuda.stream(s):
+                        op.lasso_(g, u, lam, prep[i]["step"], n_it)
+                for s in streams:
+                    cap.wait_stream(s)
+            nodes = launch_count() - n0
+            st["kernel_nodes"] += nodes
+            torch.cuda.synchronize()
+            st["capture_s"] += time.perf_counter() - t
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
             graph.replay()
-        e1.record()
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / n_steps, launch_count() - n0
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            st["solve_ms"] += ms
+            t = time.perf_counter()
+            for i, g in zip(batch, gs):
+                sols[i] = g.reshape(-1).cpu().numpy().astype(np.complex128)
+                st["d2h_bytes"] += 16 * g.numel()
+            st["d2h_s"] += time.perf_counter() - t
+            if objective:
+                t = time.perf_counter()
+                for op, g, u, lam, i in zip(ops, gs, us, lams, batch):
+                    r = op.forward(g.t().contiguous()) - u.t()
+                    obj[i] = float(0.5 * r.abs().pow(2).sum() + lam.item() * g.abs().sum())
+                t_obj += time.perf_counter() - t
+            st["batches"].append({"problems": len(batch), "gb": sum(prep[i][key] for i in batch) / 1e9,
+                                  "graph_nodes": nodes, "replay_ms": ms})
+            del graph, gs, us, lams
+            for op in ops:
+                op.close()
+            torch.cuda.empty_cache()
+        st["wall_s"] = time.perf_counter() - t_pass - t_obj
+        return st, sols, obj
 
-    precision = args.precision
-    n_launch_graph = launch_count()
-    graph = capture(precision)
-    n_launch_graph = launch_count() - n_launch_graph
     with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
         replicas_barrier(dist)
         clocks.mark_start()
-        ms, _ = timed(graph, args.steps, args.warmup)
+        st, sols, obj = solve_pass(False, objective=True)
         clocks.mark_end()
     replicas_barrier(dist)
-    ms = replicas_max_ms(dist, ms, device="cuda")
-    objective = []
-    for op, g, u, lam in zip(ops, gs, us, lams):
-        r = op.forward(g.t().contiguous()) - u.t()
-        objective.append(float(0.5 * r.abs().pow(2).sum() + lam.item() * g.abs().sum()))
-    value = world * len(ops) * n_it / (ms / 1e3)
-    g_tc = [g.clone() for g in gs]
-    line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+    ms = replicas_max_ms(dist, st["solve_ms"], device="cuda")
+    wall_ms = replicas_max_ms(dist, 1e3 * st["wall_s"], device="cuda")
+    n_total = len(probs) * n_it
+    value = n_total / (ms / 1e3)
+    st32 = sols32 = None
+    if args.fp32_steps > 0 and args.precision != "fp32":
+        st32, sols32, _ = solve_pass(True)
+    precs = [prep[i]["precision"] for i in mine]
+    line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": 1,
+            "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None,
             "dtype": {"fp32": "f32", "auto": "per problem: f32 or bf16x3 (autotuned)"}.get(
-                precision, "bf16x3 (split-BF16 operands, f32 accumulate)"),
+                args.precision, "bf16x3 (split-BF16 operands, f32 accumulate)"),
             "data": "synthetic (seeded)",
-            "config": {"workload": f"2d-lasso: first {len(ops)} of the 256 seeded uneven problems (FOV side "
-                                   f"128-512, 1-16 waves, 32-256 frequencies, 64/128 elements), {n_it} "
-                                   f"proximal-gradient LASSO iterations each, all in one CUDA graph over 4 streams; "
-                                   f"one step = one graph replay",
-                       "problems": [{"side": w.n_points_axis[0], "waves": len(w.waves), "frequencies": len(w.f),
-                                     "elements": w.n_elements} for w in probs],
-                       "plan_bytes_estimate": sum(plan_bytes_estimate(w) for w in probs),
-                       "l2": "inputs larger than L2 (tables and incident fields, GBs, re-read every iteration)"},
-            "gpu_launches": n_launch_graph * args.steps,
-            "graph": {"kernel_nodes_captured": n_launch_graph, "replays": args.steps},
-            "clocks": clocks.summary(), "plan": {"build_s": t_build}, "precision": precision,
-            "autotune": tuned or None,
-            "objective_after": objective}
-    # end to end: host FP64 data in, FP64 solution out, around one graph replay
-    u_host = [u.cpu().numpy().astype(np.complex128) for u in us]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for ub, u in zip(u_host, us):
-        u.copy_(torch.from_numpy(ub.astype(np.complex64)), non_blocking=False)
-    for g in gs:
-        g.zero_()
-    graph.replay()
-    sol = [g.cpu().numpy().astype(np.complex128) for g in gs]
-    t_e2e = time.perf_counter() - t0
-    line["e2e"] = {"value": world * len(ops) * n_it / t_e2e, "unit": "applies/s",
-                   "h2d_bytes_per_step": int(sum(8 * u.numel() for u in us)),
-                   "d2h_bytes_per_step": int(sum(8 * g.numel() for g in gs)),
-                   "path": "host FP64 measured data -> device -> one graph replay (all problems, all iterations) "
-                           "-> host FP64 solutions"}
-    del sol
-    if args.fp32_steps > 0 and precision != "fp32":
-        graph32 = capture("fp32")
-        ms32, _ = timed(graph32, args.fp32_steps, 1)
-        rel = max(float((g.cpu() - gt.cpu()).norm() / max(gt.cpu().norm(), 1e-30)) for g, gt in zip(gs, g_tc))
-        line["fp32_comparison"] = {"value": world * len(ops) * n_it / (ms32 / 1e3), "unit": "applies/s",
-                                   "ms_per_step": ms32, "steps": args.fp32_steps,
-                                   f"speedup_{precision}_over_fp32": ms32 / ms,
-                                   "max_rel_l2_solution_bf16x3_vs_fp32": rel}
+            "config": {"workload": f"2d-lasso: all {len(probs)} seeded uneven problems (FOV side 128-512, 1-16 "
+                                   f"waves, 32-256 frequencies, 64/128 elements), {n_it} proximal-gradient LASSO "
+                                   f"iterations each; batches within a {budget / 1e9:.0f} GB device-memory budget, "
+                                   f"one CUDA graph per batch over {len(streams)} streams; one step = one pass over "
+                                   f"all problems",
+                       "problems": len(probs), "iterations": n_it,
+                       "total_complex_macs_per_iteration": int(2 * sum(lasso_macs(probs[i]) for i in mine)),
+                       "l2": "inputs larger than L2 (tables and incident fields, GBs per batch, re-read every "
+                             "iteration)"},
+            "step_definition": "one pass over all problems: ms_per_step = summed graph-replay time of the batches "
+                               "(CUDA events); value = problems x iterations / that time",
+            "warmup_definition": "the preparation pass: every problem's plan built once, its data synthesised, "
+                                 "its path autotuned, its kernels run",
+            "gpu_launches": st["kernel_nodes"],
+            "graph": {"batches": st["batches"], "kernel_nodes": st["kernel_nodes"]},
+            "job": {"wall_s": st["wall_s"], "plan_build_s": st["build_s"], "h2d_s": st["h2d_s"],
+                    "capture_s": st["capture_s"], "replay_s": st["solve_ms"] / 1e3, "d2h_s": st["d2h_s"],
+                    "preparation_pass_s": t_prep},
+            "clocks": clocks.summary(), "precision": args.precision,
+            "paths": {"bf16x3": precs.count("bf16x3"), "fp32": precs.count("fp32")},
+            "objective_after": {"mean": float(np.mean(list(obj.values()))), "problems": len(obj)},
+            "e2e": {"value": n_total / (wall_ms / 1e3), "unit": "applies/s",
+                    "h2d_bytes_per_step": st["h2d_bytes"], "d2h_bytes_per_step": st["d2h_bytes"],
+                    "path": "one pass: every plan rebuilt from its setup, FP64 measured data from pinned host "
+                            "memory, one graph per batch captured and replayed, solutions back to the host"}}
+    if st32 is not None:
+        rels = [float(np.linalg.norm(sols[i] - sols32[i]) / max(np.linalg.norm(sols32[i]), 1e-30)) for i in mine]
+        line["fp32_comparison"] = {"value": n_total / (st32["solve_ms"] / 1e3), "unit": "applies/s",
+                                   "ms_per_step": st32["solve_ms"], "wall_s": st32["wall_s"],
+                                   "batches": len(st32["batches"]),
+                                   "speedup_over_fp32": st32["solve_ms"] / st["solve_ms"],
+                                   "max_rel_l2_solution_vs_fp32": max(rels),
+                                   "median_rel_l2_solution_vs_fp32": float(np.median(rels))}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and LASSO_CHECK_PROBLEM in prep:
+        line["cpu_baseline"], line["fp64_oracle_check"] = lasso_cpu_baseline(
+            probs, LASSO_CHECK_PROBLEM, prep[LASSO_CHECK_PROBLEM], n_it,
+            sols[LASSO_CHECK_PROBLEM], sols32[LASSO_CHECK_PROBLEM] if sols32 else None)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    for op in ops:
-        op.close()
     replicas_end(dist)
+
+
+def lasso_problem_oracle(w):
+    from oracle.lasso_split import lasso_problem_config
+    return lasso_problem_config(w.n_points_axis[0], w.n_elements, w.f, [a[0] for _, a in w.waves], w.density,
+                                w.seed, w.name)
+
+
+def lasso_cpu_baseline(probs, i, rec, n_it, sol, sol32):
+    """The FP64 oracle's ISTA (split over frequencies, one spawn worker per host core) on problem
+    ``i`` with the device's data: timed, scaled to the whole batch by multiply-adds, and its
+    solution compared with the device's."""
+    import numpy as np
+    from oracle.lasso_split import FrequencySplitOracle
+    w = probs[i]
+    with FrequencySplitOracle(lasso_problem_oracle(w)) as orc:
+        t0 = time.perf_counter()
+        g, _ = orc.lasso(rec["u_host"].numpy(), rec["lam"], rec["step"], n_it)
+        t = time.perf_counter() - t0
+        cores = len(orc.f_sets)
+    scale = sum(lasso_macs(p) for p in probs) / lasso_macs(w)
+    value = len(probs) * n_it / (t * scale)
+    g = g[:, 0]
+    rel = lambda x: float(np.linalg.norm(x - g) / np.linalg.norm(g))
+    base = {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
+            "sample": f"problem {i} of the batch ({w.n_points_axis[0]}x{w.n_points_axis[1]} grid, {len(w.waves)} "
+                      f"waves, {len(w.f)} frequencies, {w.n_elements} elements): {n_it} ISTA iterations of the FP64 "
+                      f"oracle (oracle.solvers.lasso_ista), frequencies split over {cores} spawn processes; whole-batch "
+                      f"rate = sample rate x that problem's multiply-adds / all problems' ({scale:.0f}x)",
+            "seconds_sample": t}
+    check = {"problem": i, "iterations": n_it, "rel_l2_solution_vs_fp64_ista": rel(sol),
+             "rel_l2_fp32_solution_vs_fp64_ista": rel(sol32) if sol32 is not None else None,
+             "what": "device LASSO solution after all iterations vs the FP64 oracle's ISTA on the same u, lambda, step"}
+    return base, check
+
+
+def run_reference_lasso(args):
+    """Reference arm of the uneven batch: the FP64 oracle's ISTA on the problem with the least work
+    (its own data: FP64 forward of gamma_true + 25 dB noise, lambda and step from the oracle), split
+    over frequencies across the host cores; each step times ``REF_LASSO_ITERS`` iterations and
+    ``value`` scales them to the whole batch by multiply-adds."""
+    import numpy as np
+    from comp_ui_toolbox_gb300.workloads import lasso_batch
+    from oracle.lasso_split import FrequencySplitOracle
+    probs = lasso_batch(args.lasso_problems)
+    i = LASSO_CHECK_PROBLEM if LASSO_CHECK_PROBLEM < len(probs) else 0
+    w = probs[i]
+    t0 = time.perf_counter()
+    with FrequencySplitOracle(lasso_problem_oracle(w)) as orc:
+        u0 = orc.forward(w.gamma(n_objects=1).real + 0j)
+        rng = np.random.default_rng(1000 + i)
+        noise = rng.standard_normal(u0.shape) + 1j * rng.standard_normal(u0.shape)
+        u = u0 + noise * (np.linalg.norm(u0) / np.linalg.norm(noise)) * 10 ** (-25 / 20)
+        lam = 0.05 * float(np.abs(orc.adjoint(u)).max())
+        x = rng.standard_normal((orc.P, 1)) + 0j
+        for _ in range(8):  # power iterations on Phi^H Phi
+            y = orc.adjoint(orc.forward(x))
+            L = float(np.linalg.norm(y) / np.linalg.norm(x))
+            x = y / np.linalg.norm(y)
+        step = 0.9 / L
+        times = []
+        g = None
+        for _ in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            g, _ = lasso_ista_from(orc, u, lam, step, REF_LASSO_ITERS, g)
+            times.append(time.perf_counter() - t)
+        cores = len(orc.f_sets)
+    wall = time.perf_counter() - t0
+    timed = sorted(times[args.warmup:])
+    t_step = timed[len(timed) // 2]
+    scale = sum(lasso_macs(p) for p in probs) / lasso_macs(w)
+    value = len(probs) * REF_LASSO_ITERS / (t_step * scale)
+    sample = (f"problem {i} of the batch: {REF_LASSO_ITERS} ISTA iterations of the FP64 oracle per step, frequencies "
+              f"split over {cores} spawn processes; whole-batch rate = sample rate x that problem's multiply-adds / "
+              f"all problems' ({scale:.0f}x)")
+    line = {"metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"2d-lasso: all {len(probs)} seeded uneven problems, {args.lasso_iters} "
+                                   f"proximal-gradient LASSO iterations each", "problems": len(probs)},
+            "impl": "reference", "extrapolated": True, "scale_factor": scale, "wall_s": wall,
+            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
+                             "host_cores": os.cpu_count(), "sample": sample},
+            "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+REF_LASSO_ITERS = 10
+
+
+def lasso_ista_from(orc, u, lam, step, n_iter, gamma0):
+    from oracle.solvers import lasso_ista
+    return lasso_ista(None, u, lam, step, n_iter, gamma0=gamma0, forward=orc.forward, adjoint=orc.adjoint,
+                      n_points=orc.P)
 
 
 def main():
@@ -792,7 +991,11 @@ def main():
     if args.table_storage is None:
         args.table_storage = {"3d": "streamed"}.get(args.workload, "auto")
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "2d-lasso":
+            if int(os.environ.get("RANK", "0")) == 0:
+                run_reference_lasso(args)
+        else:
+            run_reference(args)
     elif args.workload == "2d-lasso":
         run_lasso(args)
     else:

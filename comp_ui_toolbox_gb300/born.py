@@ -86,7 +86,9 @@ class SetupDesc(C.Structure):
                 ("width_axis", C.c_double * 2), ("n_face_axis", C.c_int32 * 2), ("absorption", AbsorptionDesc),
                 ("aa_tx_beta", C.c_double), ("aa_rx_beta", C.c_double), ("n_f_unique", C.c_int32),
                 ("f_unique", C.POINTER(C.c_double)), ("n_measurements", C.c_int32),
-                ("waves", C.POINTER(WaveDesc)), ("device", C.c_int32)]
+                ("waves", C.POINTER(WaveDesc)), ("device", C.c_int32),
+                ("face_apodization", C.POINTER(C.c_double)), ("lens_focus_axis", C.c_double * 2),
+                ("lens_c", C.c_double)]
 
 
 class BornTiming(C.Structure):
@@ -647,7 +649,8 @@ def born_forward(gamma, op: OperatorBorn):
 def setup_desc(*, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_start: float,
                n_elements_axis: Sequence[int], pitch_axis: Sequence[float], width_axis: Sequence[float],
                n_face_axis: Sequence[int], absorption: dict, f_unique, waves,
-               aa_tx_beta: Optional[float] = 0.5, aa_rx_beta: Optional[float] = 0.5, device: int = 0):
+               aa_tx_beta: Optional[float] = 0.5, aa_rx_beta: Optional[float] = 0.5, device: int = 0,
+               face_apodization=None, lens_focus_axis: Optional[Sequence[float]] = None, lens_c: float = 0.0):
     """``cui_born_setup_desc`` of a discretised setup and the arrays it points into (keep them
     alive while the descriptor is used).
 
@@ -656,6 +659,11 @@ def setup_desc(*, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_s
     frequency indices), ``v_d`` ``(F_w, E)`` normal velocities and ``mixes`` (``f_idx``,
     ``active``, ``response`` ``(F_mix, n_active)`` receive responses).  ``aa_*_beta=None``
     switches an anti-aliasing filter off.
+
+    Face weights (``face.m:234-285``): ``face_apodization`` holds the apodization at the
+    ``prod(n_face_axis)`` face points, first axis fastest (None: uniform);
+    ``lens_focus_axis`` the lens's axial focus per face axis in metres (None, 0 or inf: no
+    focusing along that axis); ``lens_c`` the lens's speed of sound (0: 1540 m/s).
     """
     keep = []
     d = SetupDesc()
@@ -700,6 +708,16 @@ def setup_desc(*, n_points_axis: Sequence[int], delta_axis: Sequence[float], z_s
     d.waves = wv
     keep.append(wv)
     d.device = int(device)
+    if face_apodization is not None:
+        fa = np.ascontiguousarray(np.asarray(face_apodization, dtype=np.float64).reshape(-1, order="F"))
+        nq = int(np.prod([max(1, int(n_face_axis[k])) for k in range(nd - 1)]))
+        if fa.size != nq:
+            raise CuiError(1, f"face_apodization has {fa.size} values, the face has {nq} points")
+        keep.append(fa)
+        d.face_apodization = fa.ctypes.data_as(C.POINTER(C.c_double))
+    for k, v in enumerate(lens_focus_axis or ()):
+        d.lens_focus_axis[k] = float(v)
+    d.lens_c = float(lens_c)
     return d, keep
 
 

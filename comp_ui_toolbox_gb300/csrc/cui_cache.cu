@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -91,6 +92,20 @@ cui_status setup_key(const cui_born_setup_desc* d, std::vector<unsigned char>& k
     put(key, ab.dispersion);
     put(key, d->aa_tx_beta);
     put(key, d->aa_rx_beta);
+    // face weights enter the key only when they are not uniform (keys of uniform setups unchanged)
+    const bool focused = (d->lens_focus_axis[0] > 0.0 && std::isfinite(d->lens_focus_axis[0])) ||
+                         (d->n_dims == 3 && d->lens_focus_axis[1] > 0.0 && std::isfinite(d->lens_focus_axis[1]));
+    if (d->face_apodization || focused) {
+        const char tag[8] = {'F', 'A', 'C', 'E', 'W', 'G', 'T', 'S'};
+        key.insert(key.end(), tag, tag + 8);
+        const size_t Q = static_cast<size_t>(std::max(1, d->n_face_axis[0])) *
+                         (d->n_dims == 3 ? static_cast<size_t>(std::max(1, d->n_face_axis[1])) : 1);
+        put(key, static_cast<int32_t>(d->face_apodization != nullptr));
+        if (d->face_apodization) put_array(key, d->face_apodization, Q);
+        put(key, d->lens_focus_axis[0]);
+        put(key, d->lens_focus_axis[1]);
+        put(key, d->lens_c);
+    }
     put_array(key, d->f_unique, static_cast<size_t>(d->n_f_unique));
     put(key, d->n_measurements);
     for (int w = 0; w < d->n_measurements; ++w) {

@@ -40,6 +40,7 @@ struct TableGen {
     const float2* sz2;  // [Nz] Z(z)^2
     const float* ax;    // [Nox] |X(ox)|
     const float* ay;    // [Noy] |Y(oy)|
+    const float2* wq;   // [F][Qy * Qx] face weights, or nullptr (uniform)
     int Nox, Noy, Qx, Qy;
     float scale;        // dA / (2 pi)
     float pitch_x, pitch_y;
@@ -54,6 +55,7 @@ struct GenRow {
     float ay2c;                  // |Y|^2 + Z^2 of the centre offsets (window distance), FP32
     float ay;                    // |Y|
     int oy;
+    int f;
 };
 
 __device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
@@ -72,6 +74,7 @@ __device__ __forceinline__ GenRow gen_row(const TableGen& t, int f, int z, int o
     r.ay = __ldg(t.ay + oy);
     r.ay2c = fmaf(r.ay, r.ay, r.z2.x);
     r.oy = oy;
+    r.f = f;
     return r;
 }
 
@@ -111,7 +114,11 @@ __device__ __forceinline__ float2 gen_entry(const TableGen& t, const GenRow& r, 
     for (int qy = 0; qy < t.Qy; ++qy) {
         const float2 yz = pair_add(__ldg(t.sy2 + static_cast<int64_t>(qy) * t.Noy + r.oy), r.z2);
         for (int qx = 0; qx < t.Qx; ++qx) {
-            const float2 g = gen_green(r, pair_add(__ldg(t.sx2 + static_cast<int64_t>(qx) * t.Nox + ox), yz));
+            float2 g = gen_green(r, pair_add(__ldg(t.sx2 + static_cast<int64_t>(qx) * t.Nox + ox), yz));
+            if (t.wq) {  // face weight w_q(f) (warp-uniform branch)
+                const float2 wv = __ldg(t.wq + (static_cast<int64_t>(r.f) * t.Qy + qy) * t.Qx + qx);
+                g = make_float2(g.x * wv.x - g.y * wv.y, g.x * wv.y + g.y * wv.x);
+            }
             acc.x += g.x;
             acc.y += g.y;
         }

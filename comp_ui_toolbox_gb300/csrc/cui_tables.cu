@@ -115,6 +115,7 @@ struct TableArgs {
     int n_dims, F, Nz, Noy, Nox, Ex, Ey, Qx, Qy;
     double dx, dy, dz, z_start, pitch_x, pitch_y, wx, wy, dA, beta;
     const double2* k;   // [F]
+    const double2* w;   // [F][Qy * Qx] face weights, or nullptr (uniform)
     float2* out;        // [F][Nz][Noy][Nox]
     int* bad;           // set when an entry is not finite
 };
@@ -148,6 +149,7 @@ __global__ void table_kernel(const TableArgs a) {
                 } else {
                     G = cscale(cexp_minus_i(kD), -1.0 / (4.0 * kPi * D));  // -exp(-j k D)/(4 pi D)
                 }
+                if (a.w) G = cmul(G, a.w[(static_cast<int64_t>(f) * a.Qy + qy) * a.Qx + qx]);
                 sum = cadd(sum, G);
             }
         }
@@ -252,9 +254,68 @@ int points_per_pitch(double pitch, double delta, bool* ok) {
 
 #define CUI_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return check_cuda(e_, #x); } while (0)
 
-// table entries of the nf frequencies whose wavenumbers start at dk, into out [nf][Nz][Noy][Nox]
-cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk, int nf, double beta, float2* out,
-                        int* dbad) {
+// Face weights w[f][q] = a_q exp(-j k_lens(f) t_q) of every frequency and face point
+// (face.m:359-376 compute_weights_scalar), q = qy * Qx + qx.  The lens thickness restates
+// thickness/focus_axial.m at the face point's normalised position rho = 2 (r_q - r_c) / width =
+// (2 q_a - Q_a + 1) / Q_a along each axis: t = sum over the focused axes of
+// (sqrt(1 + F^2) - sqrt(rho^2 + F^2)) width / 2 with F = 2 focus / width; the lens is lossless,
+// k_lens = 2 pi f / c_lens (lens.m).  Empty for uniform weights (no apodization, no focus).
+std::vector<double2> face_weights(const cui_born_setup_desc* d, int F, cui_status* st) {
+    *st = CUI_OK;
+    const int nl = d->n_dims - 1;
+    const int Qx = std::max(1, d->n_face_axis[0]), Qy = (nl == 2) ? std::max(1, d->n_face_axis[1]) : 1;
+    bool focused = false;
+    for (int a = 0; a < nl; ++a) {
+        const double fa = d->lens_focus_axis[a];
+        if (std::isnan(fa) || fa < 0.0) {
+            *st = set_error(CUI_ERR_INVALID_ARG, "lens focus must be 0, +inf or positive");
+            return {};
+        }
+        focused = focused || (fa > 0.0 && std::isfinite(fa));
+    }
+    if (!d->face_apodization && !focused) return {};
+    if (d->lens_c < 0.0 || std::isnan(d->lens_c)) {
+        *st = set_error(CUI_ERR_INVALID_ARG, "lens speed of sound must be 0 (1540 m/s) or positive");
+        return {};
+    }
+    const double c_lens = d->lens_c > 0.0 ? d->lens_c : 1540.0;
+    const int Q = Qx * Qy;
+    std::vector<double> amp(Q, 1.0), thick(Q, 0.0);
+    for (int qy = 0; qy < Qy; ++qy)
+        for (int qx = 0; qx < Qx; ++qx) {
+            const int q = qy * Qx + qx;
+            if (d->face_apodization) {
+                amp[q] = d->face_apodization[q];
+                if (!std::isfinite(amp[q])) {
+                    *st = set_error(CUI_ERR_NUMERIC, "non-finite face apodization");
+                    return {};
+                }
+            }
+            const int qa[2] = {qx, qy}, Qa[2] = {Qx, Qy};
+            for (int a = 0; a < nl; ++a) {
+                const double fa = d->lens_focus_axis[a];
+                if (!(fa > 0.0 && std::isfinite(fa))) continue;
+                const double wa = d->width_axis[a];
+                const double rho = (2.0 * qa[a] - Qa[a] + 1.0) / Qa[a];
+                const double Fn = 2.0 * fa / wa;
+                thick[q] += (std::sqrt(1.0 + Fn * Fn) - std::sqrt(rho * rho + Fn * Fn)) * wa / 2.0;
+            }
+        }
+    std::vector<double2> w(static_cast<size_t>(F) * Q);
+    for (int f = 0; f < F; ++f) {
+        const double k_lens = 2.0 * kPi * d->f_unique[f] / c_lens;
+        for (int q = 0; q < Q; ++q) {
+            const double ph = k_lens * thick[q];
+            w[static_cast<size_t>(f) * Q + q] = make_double2(amp[q] * std::cos(ph), -amp[q] * std::sin(ph));
+        }
+    }
+    return w;
+}
+
+// table entries of the nf frequencies whose wavenumbers start at dk (face weights at dw, or
+// nullptr for uniform ones), into out [nf][Nz][Noy][Nox]
+cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk, const double2* dw, int nf,
+                        double beta, float2* out, int* dbad) {
     TableArgs a;
     a.n_dims = p.n_dims; a.F = nf; a.Nz = p.Nz; a.Noy = p.Noy; a.Nox = p.Nox; a.Ex = p.Ex; a.Ey = p.Ey;
     a.Qx = std::max(1, d->n_face_axis[0]);
@@ -270,6 +331,7 @@ cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk
     a.dA = (a.wx / a.Qx) * ((p.n_dims == 3) ? a.wy / a.Qy : 1.0);
     a.beta = beta;
     a.k = dk;
+    a.w = dw;
     a.out = out;
     a.bad = dbad;
     const int64_t n = static_cast<int64_t>(nf) * p.Nz * p.Noy * p.Nox;
@@ -283,7 +345,8 @@ cui_status launch_table(Plan& p, const cui_born_setup_desc* d, const double2* dk
 // Parameters of the generated table (cui_gen.cuh): per frequency the wavenumber with its real part
 // split into an FP32 pair; per lateral offset and face quadrature point the squared distance, and per
 // row the squared depth, computed in FP64 like table_kernel and split into FP32 pairs.
-cui_status build_generator(Plan& p, const cui_born_setup_desc* d, const std::vector<double2>& k) {
+cui_status build_generator(Plan& p, const cui_born_setup_desc* d, const std::vector<double2>& k,
+                           const std::vector<double2>& wq) {
     const int Qx = std::max(1, d->n_face_axis[0]), Qy = std::max(1, d->n_face_axis[1]);
     const double dx = d->delta_axis[0], dy = d->delta_axis[1], dz = d->delta_axis[2];
     const double wx = d->width_axis[0], wy = d->width_axis[1];
@@ -334,8 +397,14 @@ cui_status build_generator(Plan& p, const cui_born_setup_desc* d, const std::vec
         (st = up(reinterpret_cast<void**>(&dax), ax.data(), sizeof(float) * ax.size())) != CUI_OK ||
         (st = up(reinterpret_cast<void**>(&day), ay.data(), sizeof(float) * ay.size())) != CUI_OK)
         return st;
+    float2* dwq = nullptr;
+    if (!wq.empty()) {  // face weights [F][Q] in FP32
+        std::vector<float2> wf(wq.size());
+        for (size_t i = 0; i < wq.size(); ++i) wf[i] = make_float2(static_cast<float>(wq[i].x), static_cast<float>(wq[i].y));
+        if ((st = up(reinterpret_cast<void**>(&dwq), wf.data(), sizeof(float2) * wf.size())) != CUI_OK) return st;
+    }
     TableGen& t = p.gen;
-    t.fk = dfk; t.sx2 = dsx; t.sy2 = dsy; t.sz2 = dsz; t.ax = dax; t.ay = day;
+    t.fk = dfk; t.sx2 = dsx; t.sy2 = dsy; t.sz2 = dsz; t.ax = dax; t.ay = day; t.wq = dwq;
     t.Nox = p.Nox; t.Noy = p.Noy; t.Qx = Qx; t.Qy = Qy;
     t.scale = static_cast<float>((wx / Qx) * (wy / Qy) / (2.0 * kPi));  // -2 dA * (-1 / (4 pi))
     t.pitch_x = static_cast<float>(d->pitch_axis[0]);
@@ -394,6 +463,9 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
     if (st != CUI_OK) return st;
     std::vector<double2> k = wavenumbers(d->absorption, d->f_unique, p.F, &st);
     if (st != CUI_OK) return st;
+    const std::vector<double2> wq = face_weights(d, p.F, &st);
+    if (st != CUI_OK) return st;
+    const int Qf = std::max(1, d->n_face_axis[0]) * ((d->n_dims == 3) ? std::max(1, d->n_face_axis[1]) : 1);
     double dV = 1.0;
     for (int a = 0; a < d->n_dims; ++a) dV *= d->delta_axis[a];
     std::vector<double2> scale(p.F);
@@ -422,6 +494,7 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
 
     // scratch for the build (released before returning)
     double2* dk = nullptr;
+    double2* dw = nullptr;
     float2* dvd = nullptr;
     int* dslot = nullptr;
     int* dbad = nullptr;
@@ -459,7 +532,7 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
         if ((st = device_alloc(p, reinterpret_cast<void**>(&p.table), tbytes)) != CUI_OK) return st;
         p.table_bytes = tbytes;
     } else {
-        if ((st = build_generator(p, d, k)) != CUI_OK) return st;
+        if ((st = build_generator(p, d, k, wq)) != CUI_OK) return st;
         p.table_bytes = 0;
         if (mode == CUI_STORAGE_STREAMED) {
             p.stream_nf = stream_nf;
@@ -494,9 +567,14 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
         (ce = talloc(reinterpret_cast<void**>(&dvd), sizeof(float2) * vd.size())) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dslot), sizeof(int) * p.S)) != cudaSuccess ||
         (ce = talloc(reinterpret_cast<void**>(&dbad), sizeof(int))) != cudaSuccess ||
-        (own_tx && (ce = talloc(reinterpret_cast<void**>(&dtx), fbytes * fchunk)) != cudaSuccess)) {
+        (own_tx && (ce = talloc(reinterpret_cast<void**>(&dtx), fbytes * fchunk)) != cudaSuccess) ||
+        (!wq.empty() && (ce = talloc(reinterpret_cast<void**>(&dw), sizeof(double2) * wq.size())) != cudaSuccess)) {
         release();
         return check_cuda(ce, "table build scratch");
+    }
+    if (!wq.empty() && (ce = cudaMemcpy(dw, wq.data(), sizeof(double2) * wq.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        release();
+        return check_cuda(ce, "face weights upload");
     }
     if ((ce = cudaMemcpy(dk, k.data(), sizeof(double2) * p.F, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (ce = cudaMemcpy(dvd, vd.data(), sizeof(float2) * vd.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -506,10 +584,11 @@ cui_status create_setup(const cui_born_setup_desc* d, int32_t max_objects, int32
         return check_cuda(ce, "table build upload");
     }
     std::vector<float2>().swap(vd);
-    if (mode == CUI_STORAGE_STORED) st = launch_table(p, d, dk, p.F, d->aa_rx_beta, p.table, dbad);
+    if (mode == CUI_STORAGE_STORED) st = launch_table(p, d, dk, dw, p.F, d->aa_rx_beta, p.table, dbad);
     for (int f0 = 0; st == CUI_OK && f0 < p.F; f0 += fchunk) {
         const int nf = std::min(fchunk, p.F - f0);
-        if (own_tx) st = launch_table(p, d, dk + f0, nf, d->aa_tx_beta, dtx, dbad);
+        if (own_tx) st = launch_table(p, d, dk + f0, dw ? dw + static_cast<size_t>(f0) * Qf : nullptr, nf, d->aa_tx_beta,
+                                      dtx, dbad);
         if (st != CUI_OK) break;
         PinArgs a;
         a.Nx = p.Nx; a.Ny = p.Ny; a.Nz = p.Nz; a.Ex = p.Ex; a.Ey = p.Ey; a.ppx = p.ppx; a.ppy = p.ppy;

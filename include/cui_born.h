@@ -169,6 +169,19 @@ typedef struct {
     int32_t n_measurements;
     const cui_wave_desc* waves;
     int32_t device;
+    /* Face weights (face.m:234-285 compute_weights; applied in setup.m:1241-1269): the lateral
+       table sums w_q(f) G(k~(f), |r - r_q|) over the face's quadrature points q, with
+       w_q(f) = a_q exp(-j k_lens(f) t_q), the same on every element.  Zero-initialised fields
+       give uniform weights (a_q = 1, t_q = 0), the table of the fields above alone. */
+    const double* face_apodization;  /* [n_face_axis[0] x n_face_axis[1]] apodization a_q at the face
+                                        points, first axis fastest: the face's apodization function
+                                        evaluated at the normalised positions 2 (r_q - r_c) / width
+                                        (face.m:210-217); NULL = uniform (apodization/uniform.m) */
+    double lens_focus_axis[2];       /* axial focus (m) per face axis of the lens thickness profile
+                                        t_q (thickness/focus_axial.m); 0 or +inf = not focused along
+                                        that axis */
+    double lens_c;                   /* speed of sound of the lens (m/s), lossless (lens.m's default
+                                        absorption model); 0 = 1540 */
 } cui_born_setup_desc;
 
 /* ---- plan lifetime ------------------------------------------------------ */

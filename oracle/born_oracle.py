@@ -29,6 +29,7 @@ __all__ = [
     "Setup", "Absorption", "Mix", "Measurement", "OperatorTables",
     "wavenumbers", "greens_function", "raised_cosine", "anti_aliasing_weights",
     "transfer_function", "shift_lateral", "lateral_table", "lateral_offsets",
+    "face_weights", "lens_thickness", "face_symmetric",
     "qpw_delays", "quantize_delays", "incident_field",
     "forward_quick_cpu", "adjoint_quick_cpu", "observation_layout",
     "T_CLK", "EPS",
@@ -78,6 +79,11 @@ class Setup:
     absorption: Absorption = Absorption()
     aa_tx_beta: Optional[float] = 0.5  # raised-cosine roll-off; None = filter off
     aa_rx_beta: Optional[float] = 0.5
+    # face weights (face.m:234-285): apodization at the face points (first axis fastest; None =
+    # uniform), the lens's axial focus per face axis (empty / 0 / inf = none) and its sound speed
+    face_apodization: Optional[tuple] = None
+    lens_focus_axis: tuple = ()
+    lens_c: float = 1540.0
 
     # ---- derived quantities -------------------------------------------------
     @property
@@ -242,25 +248,69 @@ def anti_aliasing_weights(setup: Setup, k: np.ndarray, lateral_diff: np.ndarray,
     return w
 
 
+def lens_thickness(setup: Setup) -> np.ndarray:
+    """Lens thickness at each face point (``thickness/focus_axial.m``), first axis fastest.
+
+    At the normalised position ``rho = 2 (r_q - r_c) / width`` of a face point
+    (``face.m:210-217``), ``t = sum over the focused axes of (sqrt(1 + F^2) -
+    sqrt(rho^2 + F^2)) * width / 2`` with ``F = 2 * focus / width``; an axis whose focus is
+    infinite (or 0 / absent here) adds nothing.
+    """
+    fp, _ = setup.face_points(0)
+    ctr = setup.element_centers()[0]
+    t = np.zeros(fp.shape[0])
+    for d in range(setup.n_lat):
+        focus = setup.lens_focus_axis[d] if d < len(setup.lens_focus_axis) else 0.0
+        if not (np.isfinite(focus) and focus > 0.0):
+            continue
+        w = setup.width_axis[d]
+        rho = 2.0 * (fp[:, d] - ctr[d]) / w
+        Fn = 2.0 * focus / w
+        t += (np.sqrt(1.0 + Fn ** 2) - np.sqrt(rho ** 2 + Fn ** 2)) * w / 2.0
+    return t
+
+
+def face_weights(setup: Setup, f: np.ndarray) -> np.ndarray:
+    """Complex face weights ``(F, Q)``: ``a_q exp(-1j k_lens(f) t_q)``
+    (``face.m:359-376`` ``compute_weights_scalar``) with the lens lossless,
+    ``k_lens = 2 pi f / c_lens`` (the absorption model ``none`` of ``lens.m``)."""
+    Q = int(np.prod([max(1, n) for n in setup.n_face_axis[: setup.n_lat]]))
+    a = np.ones(Q) if setup.face_apodization is None else np.asarray(setup.face_apodization, dtype=np.float64)
+    k_lens = 2.0 * np.pi * np.asarray(f, dtype=np.float64) / setup.lens_c
+    return a[None, :] * np.exp(-1j * k_lens[:, None] * lens_thickness(setup)[None, :])
+
+
+def face_symmetric(setup: Setup) -> bool:
+    """True when the face weights are even in every face axis (the symmetric-grid
+    representation ``h_ref`` + ``indices_grid_FOV_shift`` mirrors the reference element's
+    transfer function, which needs a face symmetric about its centroid)."""
+    if setup.face_apodization is None:
+        return True
+    q = tuple(max(1, n) for n in setup.n_face_axis[: setup.n_lat])
+    a = np.asarray(setup.face_apodization, dtype=np.float64).reshape(q, order="F")
+    return all(np.allclose(a, np.flip(a, axis=d), rtol=0, atol=0) for d in range(a.ndim))
+
+
 def transfer_function(setup: Setup, f: np.ndarray, e: int, beta: Optional[float],
                       points: Optional[np.ndarray] = None) -> np.ndarray:
     """Spatial transfer function of element ``e`` on the FOV grid, (F, P).
 
     ``setup.m:1216-1281`` (``transfer_function_scalar``):
-    ``h = -2 * dA * sum_q w_q G(k~ |r_q - r_p|)`` with unit apodization
-    weights (no lens thickness), followed by the anti-aliasing filter
-    (``setup.m:894-897`` -> ``on.m:64-70``).  ``points`` optionally restricts
-    the evaluation to a subset of grid indices.
+    ``h = -2 * dA * sum_q w_q(f) G(k~ |r_q - r_p|)`` with the face weights of
+    :func:`face_weights` (``setup.m:1241``, applied at ``:1266``), followed by the
+    anti-aliasing filter (``setup.m:894-897`` -> ``on.m:64-70``).  ``points``
+    optionally restricts the evaluation to a subset of grid indices.
     """
     k = wavenumbers(setup, f)
     pos = setup.positions()
     if points is not None:
         pos = pos[points]
     fp, dA = setup.face_points(e)
+    wq = face_weights(setup, f)
     h = np.zeros((len(f), pos.shape[0]), dtype=np.complex128)
     for q in range(fp.shape[0]):
         D = np.linalg.norm(pos - fp[q][None, :], axis=1)
-        h -= 2.0 * dA * greens_function(setup.n_dims, k[:, None], D[None, :])
+        h -= 2.0 * dA * wq[:, q][:, None] * greens_function(setup.n_dims, k[:, None], D[None, :])
     ctr = setup.element_centers()[e]
     diff = pos - ctr[None, :]
     dist = np.linalg.norm(diff, axis=1)
@@ -336,9 +386,10 @@ def lateral_table(setup: Setup, f: np.ndarray, beta: Optional[float]) -> np.ndar
     k = wavenumbers(setup, f)
     offs = lateral_offsets(setup)
     z = setup.axis_positions()[-1]
-    # element-0-relative face offsets (face is symmetric about its centroid)
+    # element-0-relative face offsets; the weights are the same on every element
     fp, dA = setup.face_points(0)
     fp = fp - setup.element_centers()[0][None, :]
+    wq = face_weights(setup, f)
     if setup.n_dims == 2:
         Z, X = np.meshgrid(z, offs[0][1], indexing="ij")  # (Nz, No_x)
         lat = X[..., None]
@@ -351,7 +402,8 @@ def lateral_table(setup: Setup, f: np.ndarray, beta: Optional[float]) -> np.ndar
         for d in range(setup.n_lat):
             diff_sq = diff_sq + (lat[..., d] - fp[q, d]) ** 2
         D = np.sqrt(diff_sq)
-        T -= 2.0 * dA * greens_function(setup.n_dims, k.reshape((-1,) + (1,) * Z.ndim), D[None])
+        T -= 2.0 * dA * wq[:, q].reshape((-1,) + (1,) * Z.ndim) * greens_function(
+            setup.n_dims, k.reshape((-1,) + (1,) * Z.ndim), D[None])
     dist = np.sqrt(Z ** 2 + np.sum(lat ** 2, axis=-1))
     T *= anti_aliasing_weights(setup, k, lat, dist, beta)
     return T

@@ -16,7 +16,7 @@ from typing import Optional
 import numpy as np
 
 from .born_oracle import (
-    Absorption, Measurement, Mix, OperatorTables, Setup, incident_field, lateral_table,
+    Absorption, Measurement, Mix, OperatorTables, Setup, face_symmetric, incident_field, lateral_table,
     qpw_delays, quantize_delays, shift_lateral, transfer_function, wavenumbers,
 )
 
@@ -236,6 +236,7 @@ def build(cfg: BornConfig, direct_elements: bool = False) -> BuiltOperator:
             mixes.append(Mix(f_idx=mf, active=active, pref=(-s.cell_volume * kk ** 2)[:, None] * resp))
         measurements.append(Measurement(f_idx=f_idx, p_incident=p_in, mixes=mixes))
     shift, valid = shift_lateral(s)
+    valid = valid and face_symmetric(s)  # mirroring h_ref needs a face symmetric about its centroid
     op = OperatorTables(setup=s, f_unique=f, measurements=measurements)
     if valid:
         op.h_ref = transfer_function(s, f, 0, s.aa_rx_beta)

@@ -35,20 +35,29 @@ def soft_threshold(v: np.ndarray, s) -> np.ndarray:
     return v * scale
 
 
-def lasso_ista(op: OperatorTables, u: np.ndarray, lam, step: float, n_iter: int, gamma0=None):
+def lasso_ista(op: OperatorTables, u: np.ndarray, lam, step: float, n_iter: int, gamma0=None,
+               forward=None, adjoint=None, n_points: int | None = None):
     """``n_iter`` ISTA iterations per column of ``u``; returns ``(gamma, loss)`` where ``loss``
-    is ``0.5||Phi gamma_k - u||^2`` of the last iteration's input iterate (per column)."""
+    is ``0.5||Phi gamma_k - u||^2`` of the last iteration's input iterate (per column).
+    ``forward``/``adjoint`` (callables on FP64 arrays, with ``n_points``) replace the oracle
+    operator ``op``, e.g. by one split over processes."""
+    if forward is None:
+        def forward(x):
+            return forward_quick_cpu(op, x)
+
+        def adjoint(y):
+            return adjoint_quick_cpu(op, y)
     u = np.asarray(u, dtype=np.complex128)
     u2 = u[:, None] if u.ndim == 1 else u
     B = u2.shape[1]
-    P = op.setup.n_points
+    P = op.setup.n_points if n_points is None else n_points
     g = np.zeros((P, B), dtype=np.complex128) if gamma0 is None else np.array(gamma0, dtype=np.complex128).reshape(P, B)
     lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (B,))
     loss = np.zeros(B)
     for _ in range(n_iter):
-        r = forward_quick_cpu(op, g) - u2
+        r = forward(g) - u2
         loss = 0.5 * np.sum(np.abs(r) ** 2, axis=0)
-        g = soft_threshold(g - step * adjoint_quick_cpu(op, r), step * lam[None, :])
+        g = soft_threshold(g - step * adjoint(r), step * lam[None, :])
     return g, loss
 
 

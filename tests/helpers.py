@@ -50,4 +50,5 @@ def setup_kwargs(cfg: configs.BornConfig) -> dict:
     return dict(n_points_axis=s.n_points_axis, delta_axis=s.delta_axis, z_start=s.z_start,
                 n_elements_axis=s.n_elements_axis, pitch_axis=s.pitch_axis[:nl], width_axis=s.width_axis[:nl],
                 n_face_axis=s.n_face_axis[:nl], absorption=absorption, f_unique=f, waves=waves,
-                aa_tx_beta=s.aa_tx_beta, aa_rx_beta=s.aa_rx_beta)
+                aa_tx_beta=s.aa_tx_beta, aa_rx_beta=s.aa_rx_beta, face_apodization=s.face_apodization,
+                lens_focus_axis=tuple(s.lens_focus_axis), lens_c=s.lens_c)

@@ -106,3 +106,38 @@ def test_unknown_table_storage_is_rejected_on_the_host():
     from tests.helpers import setup_kwargs
     with pytest.raises(KeyError):
         OperatorBorn.from_setup(**setup_kwargs(configs.small_config("c3")), table_storage="compressed")
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every struct the Python mirror passes through the C-ABI has the header's size and field
+    offsets (a C program compiled against include/cui_born.h prints them)."""
+    import json
+    import shutil
+    import subprocess
+    from comp_ui_toolbox_gb300 import born
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"cui_mix_desc": born.MixDesc, "cui_measurement_desc": born.MeasurementDesc,
+             "cui_born_desc": born.BornDesc, "cui_absorption_desc": born.AbsorptionDesc,
+             "cui_wave_desc": born.WaveDesc, "cui_born_setup_desc": born.SetupDesc,
+             "cui_born_timing": born.BornTiming, "cui_born_info": born.BornInfo}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "cui_born.h"', "int main(void) {",
+             'printf("{");']
+    first = True
+    for cname, py in pairs.items():
+        for fname, _ in py._fields_:
+            sep = "" if first else ","
+            first = False
+            lines.append(f'printf("{sep}\\"{cname}.{fname}\\": %zu", offsetof({cname}, {fname}));')
+        lines.append(f'printf(",\\"{cname}\\": %zu", sizeof({cname}));')
+    lines += ['printf("}\\n");', "return 0; }"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", f"-I{HEADER.parent}", str(src), "-o", str(exe)], check=True)
+    got = json.loads(subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout)
+    for cname, py in pairs.items():
+        assert got[cname] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[f"{cname}.{fname}"] == getattr(py, fname).offset, f"{cname}.{fname}"
