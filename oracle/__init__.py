@@ -10,12 +10,17 @@ The package restates, in numpy/scipy FP64, the reference toolbox's
 (mschiffn/comp_ui_toolbox) CPU Born operator and the table builders that
 feed it.  Every function cites the reference file:line it follows.
 
-Parity status: the reference is MATLAB-only and none of its scripts pin
-numbers on this path (no golden vectors, no fixtures, no asserts), so the
-restatement is checked against mathematics (mpmath Hankel functions at 30
-digits, the dot-product adjointness test, the reference's own symmetric-grid
-index map against direct per-element evaluation) rather than against outputs
-of the reference itself: parity unpinned.
+Parity status: pinned against the reference itself.  The reference's MEX
+gateway ``+scattering/combined_quick_gpu.cu`` compiles unchanged on the host
+against the stub MEX and CUDA runtimes of ``oracle/ref_mex`` (its device kernel
+``compute_matrix_kernel``, ``:1099-1124``, runs as a host restatement, and
+``cublasCgemm`` as a host FP32 complex GEMM).  Its outputs on the small
+configurations are frozen in ``tests/golden/reference_gateway.npz``
+(``tests/golden/make_reference_golden.py``), and the oracle agrees with them to
+FP32 rounding (relative L2 <= 1e-6; ``tests/test_reference_pinning.py``).  The
+restatement is also checked against mathematics: mpmath Hankel functions at 30
+digits, the dot-product adjointness test, and the reference's symmetric-grid
+index map against direct per-element evaluation.
 """
 
 from .born_oracle import *  # noqa: F401,F403
