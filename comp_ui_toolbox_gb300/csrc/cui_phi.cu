@@ -59,6 +59,8 @@ namespace {
 
 constexpr int kPhiObj = 64;          // objects per GEMM pass
 constexpr int kPieceGroup = 512;     // bytes of (c, hl) x 8 rows for one row octet and point block
+constexpr int kPbPad = 0;            // bytes between the 16 KB chunks of consecutive point blocks
+constexpr int64_t kPbStride = 32 * kPieceGroup + kPbPad;  // bytes per (256-row block, point block) chunk
 constexpr int kKStepA = 16384;       // A bytes per K step: 32 octets (256 rows or 256 points) x 512 B
 constexpr int kKStepB = 8192;        // B bytes per K step: 256 N rows x 16 K x 2 B
 constexpr uint64_t kDrainNs = 1000000000ull;
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs a) {
             split1(ph.x, v[0][k], v[1][k]);
             split1(ph.y, v[2][k], v[3][k]);
         }
-        uint8_t* dst = a.phi + ((((a.r0 >> 8) + RBl) * a.npb + pb) * 32 + rbl) * kPieceGroup + rr * 16;
+        uint8_t* dst = a.phi + (((a.r0 >> 8) + RBl) * a.npb + pb) * kPbStride + rbl * kPieceGroup + rr * 16;
         *reinterpret_cast<uint4*>(dst) = pack8(v[0]);        // re hi
         *reinterpret_cast<uint4*>(dst + 128) = pack8(v[1]);  // re lo
         *reinterpret_cast<uint4*>(dst + 256) = pack8(v[2]);  // im hi
@@ -294,16 +296,19 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
             if (lane == 0) tc::bar_expect_tx(FULL + 8 * s, C::STAGE);
             __syncwarp();
             if (!ADJ) {
-                if (lane == 0) {
-                    tc::bulk_g2s(sa, a.phi + ((tile * a.npb + k0) * 32) * kPieceGroup, C::A_BYTES, FULL + 8 * s);
-                    tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
+                if (kPbPad == 0) {  // the stage's KS point-block chunks are one contiguous run
+                    if (lane == 0) tc::bulk_g2s(sa, a.phi + (tile * a.npb + k0) * kPbStride, C::A_BYTES, FULL + 8 * s);
+                } else if (lane < KS) {
+                    tc::bulk_g2s(sa + lane * kKStepA, a.phi + (tile * a.npb + k0 + lane) * kPbStride, kKStepA,
+                                 FULL + 8 * s);
                 }
+                if (lane == 0) tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
             } else {
                 // K steps k0..k0+KS-1 are row octets of one 256-row block (KS divides 32)
                 const int64_t RB = k0 >> 5, rbl0 = k0 & 31;
                 const int64_t pbk = tile * 32 + lane;  // this lane's point block
                 tc::bulk_g2s(sa + lane * (KS * kPieceGroup),
-                             a.phi + ((RB * a.npb + pbk) * 32 + rbl0) * kPieceGroup, KS * kPieceGroup, FULL + 8 * s);
+                             a.phi + (RB * a.npb + pbk) * kPbStride + rbl0 * kPieceGroup, KS * kPieceGroup, FULL + 8 * s);
                 if (lane == 0) tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
             }
             last[s] = q / NS;
@@ -432,7 +437,7 @@ cui_status copy_back(std::vector<T>& h, const T* d, size_t n) {
 // ---------------------------------------------------------------------------
 size_t phi_matrix_bytes(const Plan* p) {
     const int64_t rows = (p->n_obs + 255) / 256 * 256, pts = (p->P + 255) / 256 * 256;
-    return static_cast<size_t>(rows) * static_cast<size_t>(pts) * 8;
+    return static_cast<size_t>(rows / 256) * static_cast<size_t>(pts / 8) * static_cast<size_t>(kPbStride);
 }
 
 bool phi_supported(const Plan* p, std::string* why) {
