@@ -171,6 +171,7 @@ struct Plan {
     size_t phi_bytes = 0;
     int64_t phi_rows_pad = 0;
     int64_t phi_npb = 0;             // 8-point blocks
+    uint64_t phi_tmap[16] = {};      // the adjoint's tensor map over the folded matrix (a CUtensorMap, 128 B)
     int64_t phi_reps = 0;            // distinct element sums the build formed
     int phi_fwd_kc = 1, phi_adj_kc = 1;
     uint8_t* phi_gforms = nullptr;

@@ -24,7 +24,9 @@
 // and an MN-major A tile of the adjoint (M = points, K = rows), so one copy of
 // the matrix serves both directions:
 //   forward, per 8-point K step: 256 rows x (c, hl) are one contiguous 16 KB;
-//   adjoint, per 8-row K step: 256 points are 32 pieces of 512 B, 16 KB apart.
+//   adjoint, per 8-row K step: 256 points are 32 pieces of 512 B, 16 KB apart, so an
+//   adjoint stage of KS row octets is one 4D tensor copy (box: 32 point blocks x KS
+//   row octets x 512 B) whose shared-memory order is the MN-major A tile.
 // K steps take the two components as two 8-element halves: K = [8 x re | 8 x im].
 // The other operand is written once per apply in its shared-memory layout
 // (K-major, N rows = [B1 hi | B2 hi | B1 lo | B2 lo] x 64 objects):
@@ -34,13 +36,14 @@
 // A lo x B hi) accumulate hi*hi + hi*lo + lo*hi into the same 128 FP32 columns
 // [Re 64 | Im 64] of tensor memory.
 //
-// Block: 10 warps.  Warp 9 issues the bulk copies, lane 0 of warp 8 the MMAs
+// Block: 10 warps.  Warp 9 issues the bulk and tensor copies, lane 0 of warp 8 the MMAs
 // (warp 8 also owns the tensor memory: 2 tiles x 2 buffers x 128 columns), and
 // warps 0-7 read the accumulators out: the tensor cores' FP32 accumulation loses
 // precision over long chains, so every 32 K steps a chain's accumulator is
 // handed over and added into FP32 registers while the MMAs continue in the
 // tile's other buffer.  Every wait has a wall-clock limit after which the block
 // drains its copies and MMAs, raises the plan's status word and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -243,7 +246,8 @@ __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatil
 // ADJ = false: block (kc, row block RB) contracts its 256 rows over the point range of chunk kc.
 // ADJ = true: block (point block PS, kc) contracts its 256 points over the row range of chunk kc.
 template <bool ADJ, int KS, int NS>
-__global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmArgs a) {
+__global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmArgs a,
+                                                                  const __grid_constant__ CUtensorMap tmap) {
     using C = PhiCfg<KS, NS>;
     static_assert(kChain % KS == 0, "chains end on stage boundaries");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -304,12 +308,13 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
                 }
                 if (lane == 0) tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
             } else {
-                // K steps k0..k0+KS-1 are row octets of one 256-row block (KS divides 32)
-                const int64_t RB = k0 >> 5, rbl0 = k0 & 31;
-                const int64_t pbk = tile * 32 + lane;  // this lane's point block
-                tc::bulk_g2s(sa + lane * (KS * kPieceGroup),
-                             a.phi + (RB * a.npb + pbk) * kPbStride + rbl0 * kPieceGroup, KS * kPieceGroup, FULL + 8 * s);
-                if (lane == 0) tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
+                // K steps k0..k0+KS-1 are row octets of one 256-row block (KS divides 32): one tensor copy
+                // of the box [point block 32][row octet KS][512 B] lands as the MN-major A stage
+                if (lane == 0) {
+                    const int RB = static_cast<int>(k0 >> 5), rbl0 = static_cast<int>(k0 & 31);
+                    tc::tma_load_4d(sa, &tmap, 0, rbl0, static_cast<int>(tile * 32), RB, FULL + 8 * s);
+                    tc::bulk_g2s(sb, a.bf + k0 * kKStepB, C::B_BYTES, FULL + 8 * s);
+                }
             }
             last[s] = q / NS;
         }
@@ -405,9 +410,11 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
 }
 
 // Stage shapes (K steps per stage, stages), measured on the batched workload at 64 frequencies
-// (68.7 GB matrix): the forward streams 6.76 TB/s with 4 x 2, 6.55 with 2 x 4 and 5.59 with 1 x 8;
-// the adjoint gathers 32 point-block pieces of KS x 512 B per stage, and its rate follows the piece
-// size: 5.39 TB/s with 2 KB pieces (4 x 2), 4.06 with 1 KB (2 x 4), 2.13 with 512 B (1 x 8).
+// (68.7 GB matrix): the forward streams 6.76 TB/s with 4 x 2, 6.55 with 2 x 4 and 5.59 with 1 x 8.
+// The adjoint's stage is 32 point-block pieces of KS x 512 B.  Issued as 32 bulk copies its rate
+// followed the piece size (5.39 TB/s at 2 KB pieces, 4.06 at 1 KB, 2.13 at 512 B; padding the
+// 16 KB stride changed nothing): the copies' issue, not DRAM, bounded it.  As one tensor copy per
+// stage it streams 5.82 TB/s at 4 x 2; 8 x 1 (one 192 KB stage, no overlap) falls to 3.90.
 constexpr int kFwdKS = 4, kFwdNS = 2;
 constexpr int kAdjKS = 4, kAdjNS = 2;
 
@@ -431,6 +438,44 @@ cui_status copy_back(std::vector<T>& h, const T* d, size_t n) {
 }
 
 }  // namespace
+
+// The adjoint's tensor map over the folded matrix, a 4D tensor of 16-bit elements, innermost first:
+// 256 (the 512 B of one row octet and point block), 32 row octets of a 256-row block (stride
+// 512 B), the point blocks (stride kPbStride) and the 256-row blocks (stride NPB x kPbStride).  A
+// box of [256, KS, 32, 1] at (0, row octet, first point block, row block) is one adjoint stage:
+// 32 point blocks x KS row octets x 512 B, in shared memory in the order the MN-major descriptor
+// reads.  Every box lies inside the tensor (row octets + KS <= 32, point blocks padded to 256).
+static cui_status encode_adjoint_map(Plan& p) {
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return set_error(CUI_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = reinterpret_cast<Encode>(fn);
+    }
+    static_assert(sizeof(CUtensorMap) == sizeof(p.phi_tmap), "tensor map storage");
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(kPieceGroup / 2), 32, static_cast<cuuint64_t>(p.phi_npb),
+                                static_cast<cuuint64_t>(p.phi_rows_pad / 256)};
+    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(kPieceGroup), static_cast<cuuint64_t>(kPbStride),
+                                   static_cast<cuuint64_t>(p.phi_npb) * static_cast<cuuint64_t>(kPbStride)};
+    const cuuint32_t box[4] = {static_cast<cuuint32_t>(kPieceGroup / 2), static_cast<cuuint32_t>(kAdjKS), 32, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (p.phi_npb % 32 != 0 || 32 % kAdjKS != 0 || (reinterpret_cast<uintptr_t>(p.phi) & 15) != 0)
+        return set_error(CUI_ERR_UNSUPPORTED_SETUP, "folded matrix layout does not tile into adjoint stages");
+    CUtensorMap m;
+    const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, p.phi, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(CUI_ERR_CUDA, "cuTensorMapEncodeTiled failed for the folded matrix (" + std::to_string(r) + ")");
+    std::memcpy(p.phi_tmap, &m, sizeof m);
+    return CUI_OK;
+}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -531,6 +576,7 @@ cui_status phi_build(Plan& p) {
     p.phi_bytes = phi_matrix_bytes(&p);
     cudaError_t e = cudaSuccess;
     if ((st = device_alloc(p, reinterpret_cast<void**>(&p.phi), p.phi_bytes)) != CUI_OK) return st;
+    if ((st = encode_adjoint_map(p)) != CUI_OK) return st;
 
     // element sums per chunk of 256-row blocks, as many representatives at a time as fit a
     // temporary of at most 16 GiB (every representative at once for the benchmark plans)
@@ -665,8 +711,11 @@ cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cud
     a.phi = p->phi; a.bf = p->phi_gforms; a.npb = p->phi_npb; a.nrb8 = p->phi_rows_pad / 8; a.n_kc = p->phi_fwd_kc;
     a.B = B; a.n_out = p->n_obs; a.part = p->phi_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
     if ((e = timing_begin(p, 0, st)) != cudaSuccess) return e;
+    CUtensorMap unused;  // the forward's stages are contiguous runs (plain bulk copies)
+    std::memset(&unused, 0, sizeof unused);
     phi_gemm_kernel<false, kFwdKS, kFwdNS>
-        <<<dim3(p->phi_fwd_kc, static_cast<unsigned>(p->phi_rows_pad / 256)), kPhiThreads, PhiCfg<kFwdKS, kFwdNS>::SMEM, st>>>(a);
+        <<<dim3(p->phi_fwd_kc, static_cast<unsigned>(p->phi_rows_pad / 256)), kPhiThreads, PhiCfg<kFwdKS, kFwdNS>::SMEM, st>>>(
+            a, unused);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = timing_end(p, st)) != cudaSuccess) return e;
@@ -686,8 +735,11 @@ cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStr
     a.phi = p->phi; a.bf = p->phi_uforms; a.npb = p->phi_npb; a.nrb8 = nrb8; a.n_kc = p->phi_adj_kc;
     a.B = B; a.n_out = p->P; a.part = p->phi_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
     if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
+    CUtensorMap tmap;
+    std::memcpy(&tmap, p->phi_tmap, sizeof tmap);
     phi_gemm_kernel<true, kAdjKS, kAdjNS>
-        <<<dim3(static_cast<unsigned>(p->phi_npb / 32), p->phi_adj_kc), kPhiThreads, PhiCfg<kAdjKS, kAdjNS>::SMEM, st>>>(a);
+        <<<dim3(static_cast<unsigned>(p->phi_npb / 32), p->phi_adj_kc), kPhiThreads, PhiCfg<kAdjKS, kAdjNS>::SMEM, st>>>(
+            a, tmap);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = timing_end(p, st)) != cudaSuccess) return e;

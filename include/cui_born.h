@@ -270,9 +270,10 @@ cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int
  * exit, so slots x n_objects x elements x 16 B must not exceed 16 MiB, and
  * n_objects x (slot passes of the widest frequency) must not exceed 65535
  * (else CUI_ERR_INVALID_ARG).  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (other streams, other plans, other threads) race. */
+ * array's device address (cudaGetSymbolAddress) and keeps it for devices 0-63
+ * (a plan on a higher device index: CUI_ERR_INVALID_ARG).  All calls share the
+ * array: calls that overlap on the GPU (other streams, other plans, other
+ * threads) race. */
 cui_status cui_born_forward_static(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
                                    int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream);
 
