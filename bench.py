@@ -183,6 +183,50 @@ def time_greedy(op):
             "data": "16 seeded point scatterers, noiseless"}
 
 
+def occupancy_sweep(op, densities=(0.001, 0.005, 0.02, 0.05, 0.0625, 0.1, 0.25, 1.0)):
+    """FP32 forward of one column against the density of gamma's nonzeros.
+
+    The reference's forward contracts only the occupied grid points (``operator_born.m:361``,
+    ``combined_quick_gpu.cu:457-499``).  The plan lists them on the device and takes the
+    compacted contraction at up to N_points/16 of them, otherwise the dense kernels.  For each
+    density (seeded positions, N(0,1) values) this times 10 forwards with CUDA events, notes the
+    path, and checks the result against the dense kernels on the same gamma (occupancy limit 0).
+    """
+    import numpy as np
+    import torch
+    prev = op.precision
+    op.set_precision("fp32")
+    P = op.n_points
+    rng = np.random.default_rng(5)
+    rows = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for d in densities:
+        nnz = max(1, int(round(d * P)))
+        g = np.zeros((P, 1), dtype=np.complex64)
+        g[rng.choice(P, nnz, replace=False), 0] = rng.standard_normal(nnz)
+        gt = torch.from_numpy(g).cuda()
+        op.set_occupancy_limit(-1)
+        for _ in range(2):
+            u = op.forward(gt)
+        torch.cuda.synchronize()
+        e0.record(torch.cuda.current_stream())
+        for _ in range(10):
+            u = op.forward(gt)
+        e1.record(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        op.set_occupancy_limit(0)
+        u_dense = op.forward(gt)
+        op.set_occupancy_limit(-1)
+        rows.append({"density": d, "nnz": nnz, "forward_ms": ms,
+                     "path": "compacted" if nnz <= P // 16 else "dense",
+                     "rel_l2_vs_dense": float((u - u_dense).norm() / u_dense.norm())})
+    op.set_precision(prev)
+    return {"rows": rows, "threshold_points": P // 16,
+            "what": "FP32 forward of one seeded gamma column per density: ms per forward (CUDA events, 10 "
+                    "forwards), the path taken, and the relative L2 difference from the dense kernels"}
+
+
 def roofline_of(args, info, kt, B, clk, p_used: float = 1.0):
     """Roofline of the dominant contraction kernel of one apply.
 
@@ -626,6 +670,8 @@ def run_ours(args):
     if args.workload in ("2d-gradient", "2d-plain") and not args.no_greedy:
         line["greedy"] = time_greedy(op)
         line["greedy"]["precision"] = args.precision
+    if B == 1 and args.n_freq is None:
+        line["occupancy_sweep"] = occupancy_sweep(op)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             # the check needs the full workload: the oracle's sample takes its frequencies from the full list

@@ -334,6 +334,7 @@ class OperatorBorn:
         self.n_points = self.info["n_points"]
         self.device = int(device)
         self.table_storage = "stored"
+        self.precision = "fp32"  # the path a new plan runs (cui_born_set_precision changes it)
 
     # ------------------------------------------------------------------
     def close(self):
@@ -373,7 +374,8 @@ class OperatorBorn:
         _check(self._lib.cui_born_autotune(self._plan, int(n_objects), C.byref(choice), ms, st))
         tiles, fwd, adj = C.c_int32(0), C.c_int32(0), C.c_int32(0)
         _check(self._lib.cui_born_autotune_config(self._plan, C.byref(tiles), C.byref(fwd), C.byref(adj)))
-        return {"precision": "bf16x3" if choice.value == 1 else "fp32", "ms_fp32": ms[0], "ms_bf16x3": ms[1],
+        self.precision = "bf16x3" if choice.value == 1 else "fp32"  # the plan now runs the kept path
+        return {"precision": self.precision, "ms_fp32": ms[0], "ms_bf16x3": ms[1],
                 "launch_shapes": {"narrow_tiles": tiles.value, "fwd_blocks": fwd.value or "rule",
                                   "adj_blocks": adj.value or "rule"}}
 
