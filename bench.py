@@ -382,8 +382,8 @@ class ClockSampler:
 
 # bounded CPU samples (about 10-30 s of host work): (waves, frequencies, receive mixes or None = all,
 # axial planes or None = all); "cores" = one receive mix per host core (the 32 mixes of 2d-batched)
-CPU_SAMPLE = {"2d-plain": (1, 8, None, None), "2d-gradient": (1, 8, None, None), "2d-batched": (1, 1, "cores", None),
-              "3d": (1, 1, None, 4)}
+CPU_SAMPLE = {"2d-plain": (1, 64, None, None), "2d-gradient": (1, 96, None, None), "2d-batched": (1, 1, "cores", None),
+              "3d": (1, 2, None, None)}
 # per-step samples of the reference arm, small enough for --steps K --warmup W to end within minutes
 REF_SAMPLE = {"2d-plain": (1, 2, None, None), "2d-gradient": (1, 1, None, 128), "2d-batched": (1, 1, "cores", 128),
               "3d": (1, 1, None, 2)}

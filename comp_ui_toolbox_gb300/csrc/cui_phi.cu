@@ -414,9 +414,10 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
 // The adjoint's stage is 32 point-block pieces of KS x 512 B.  Issued as 32 bulk copies its rate
 // followed the piece size (5.39 TB/s at 2 KB pieces, 4.06 at 1 KB, 2.13 at 512 B; padding the
 // 16 KB stride changed nothing): the copies' issue, not DRAM, bounded it.  As one tensor copy per
-// stage it streams 5.82 TB/s at 4 x 2; 8 x 1 (one 192 KB stage, no overlap) falls to 3.90.
+// stage it streams 6.38 TB/s at 2 x 4, 5.97 at 4 x 2 and 5.25 at 1 x 8; 8 x 1 (one 192 KB stage,
+// no overlap of copy and MMA) falls to 3.90.
 constexpr int kFwdKS = 4, kFwdNS = 2;
-constexpr int kAdjKS = 4, kAdjNS = 2;
+constexpr int kAdjKS = 2, kAdjNS = 4;
 
 int grid_1d(int64_t n, int threads) {
     const int64_t b = (n + threads - 1) / threads;
