@@ -2,8 +2,9 @@
 
 The reference's forward contracts only the grid points where some column of gamma is nonzero
 (``operator_born.m:361``, ``combined_quick_gpu.cu:457-499``).  The library lists those points on
-the device and, when at most the plan's limit (default N_points / 16) are occupied, contracts over
-the list instead of the dense grid.  Checks against the FP64 oracle (relative L2 <= 1e-5 per
+the device and, when at most the plan's limit (default N_points / 16 with a stored table, / 32 with
+a streamed or generated one) are occupied, contracts over the list instead of the dense grid, the
+occupied points split into chunks whose partial sums are added in a fixed order.  Checks against the FP64 oracle (relative L2 <= 1e-5 per
 column) and against the dense kernels of the same plan: sparse and ragged occupancy, several
 columns whose union decides, an all-zero gamma, a union above the limit (the dense path runs),
 3D plans with stored, streamed and generated tables, and the LASSO loop whose iterates the
@@ -92,3 +93,24 @@ def test_lasso_with_compacted_forwards_matches_dense():
         op.close()
     assert np.abs(out[0]).max() > 0
     assert rel_l2(out[-1], out[0]) <= 1e-4
+
+
+@pytest.mark.parametrize("name,storage", [("2d-gradient", "auto"), ("3d", "streamed")])
+def test_compacted_forward_at_the_limit_full_size(name, storage):
+    """Full-size plans with exactly the default limit's number of occupied points (the longest
+    sums the compacted forward forms) against the dense kernels of the same plan (which the
+    full-size parity tests pin to the FP64 oracle)."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+    w = workload(name)
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=1, table_storage=storage)
+    P = op.n_points
+    n_occ = P // (16 if op.table_storage == "stored" else 32)
+    g = dev(sparse_gamma(P, 1, n_occ, 41))
+    u = op.forward(g).cpu().numpy()
+    op.set_occupancy_limit(0)
+    u_dense = op.forward(g).cpu().numpy()
+    assert rel_l2(u, u_dense) <= TOL
+    op.set_occupancy_limit(n_occ - 1)  # one point above the limit: the dense kernels run
+    assert rel_l2(op.forward(g).cpu().numpy(), u_dense) == 0.0
+    op.close()
