@@ -188,7 +188,8 @@ def occupancy_sweep(op, densities=(0.001, 0.005, 0.02, 0.05, 0.0625, 0.1, 0.25, 
 
     The reference's forward contracts only the occupied grid points (``operator_born.m:361``,
     ``combined_quick_gpu.cu:457-499``).  The plan lists them on the device and takes the
-    compacted contraction at up to N_points/16 of them, otherwise the dense kernels.  For each
+    compacted contraction at up to N_points/16 of them (N_points/32 when the table is streamed or
+    generated), otherwise the dense kernels.  For each
     density (seeded positions, N(0,1) values) this times 10 forwards with CUDA events, notes the
     path, and checks the result against the dense kernels on the same gamma (occupancy limit 0).
     """
@@ -197,6 +198,7 @@ def occupancy_sweep(op, densities=(0.001, 0.005, 0.02, 0.05, 0.0625, 0.1, 0.25, 
     prev = op.precision
     op.set_precision("fp32")
     P = op.n_points
+    limit = P // (16 if op.table_storage == "stored" else 32)  # the plan's default limit
     rng = np.random.default_rng(5)
     rows = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -219,10 +221,10 @@ def occupancy_sweep(op, densities=(0.001, 0.005, 0.02, 0.05, 0.0625, 0.1, 0.25, 
         u_dense = op.forward(gt)
         op.set_occupancy_limit(-1)
         rows.append({"density": d, "nnz": nnz, "forward_ms": ms,
-                     "path": "compacted" if nnz <= P // 16 else "dense",
+                     "path": "compacted" if nnz <= limit else "dense",
                      "rel_l2_vs_dense": float((u - u_dense).norm() / u_dense.norm())})
     op.set_precision(prev)
-    return {"rows": rows, "threshold_points": P // 16,
+    return {"rows": rows, "threshold_points": limit,
             "what": "FP32 forward of one seeded gamma column per density: ms per forward (CUDA events, 10 "
                     "forwards), the path taken, and the relative L2 difference from the dense kernels"}
 

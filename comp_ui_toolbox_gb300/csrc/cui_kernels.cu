@@ -265,9 +265,11 @@ __global__ void __maxnreg__(NC * KE >= 16 ? 128 : 80) fwd_dense3_kernel(const Fw
 }
 
 // G[s][b][e] = sum over line groups of the forward partials (skipped when the compacted forward ran)
+// G = sum over the partials part[k][n] in order k = 0, 1, ...: `groups` of them written by the
+// dense kernels, or `sparse_groups` by the compacted forward when the device chose it (occ_sel)
 __global__ void reduce_groups_kernel(const float2* __restrict__ part, int groups, int64_t n, float2* __restrict__ G,
-                                     const int* occ_sel = nullptr) {
-    if (occ_sel && *occ_sel != 0) return;
+                                     const int* occ_sel = nullptr, int sparse_groups = 0) {
+    if (occ_sel && *occ_sel != 0) groups = sparse_groups;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         float2 s = make_float2(0.f, 0.f);
@@ -1040,21 +1042,26 @@ struct SparseFwdArgs {
     const int* __restrict__ idx;
     const int* __restrict__ cnt;       // n_occ at [2 nblk], the choice at [2 nblk + 1]
     int nblk, B;
-    float2* __restrict__ G;            // [S][B][E]
+    int n_chunks;                      // point chunks: gridDim.z
+    float2* __restrict__ part;         // [n_chunks][S][B][E] partial sums
 };
 
 constexpr int kSpThreads = 256;
 constexpr int kSpMaxPerThread = 4;  // elements per thread: arrays of up to 1024 elements
 
-// G[s][b][e] = sum over the occupied points p of h(f_s; o(p, e), z_p) p_in[s][p] gamma[b][p]:
-// block per (slot, object), thread per element (up to 4), the points staged 256 at a time with
-// their q = p_in gamma and grid coordinates
+// part[c][s][b][e] = sum over chunk c of the occupied points p of h(f_s; o(p, e), z_p) p_in[s][p]
+// gamma[b][p]: block per (slot, object, point chunk), thread per element (up to 4), the chunk's
+// points staged 256 at a time with their q = p_in gamma and grid coordinates.  Each staged batch
+// is summed on its own and then added to the chunk's total (two-level summation), and the chunks
+// are added in order by reduce_groups_kernel, so no accumulation chain runs over all points.
 template <bool GEN>
 __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdArgs a) {
     if (a.cnt[2 * a.nblk + 1] == 0) return;  // the dense kernels run instead
     const LineGeom& g = a.g;
-    const int s = blockIdx.x, b = blockIdx.y, f = a.slot_f[s];
+    const int s = blockIdx.x, b = blockIdx.y, c = blockIdx.z, f = a.slot_f[s];
     const int n_occ = a.cnt[2 * a.nblk];
+    const int per = (n_occ + a.n_chunks - 1) / a.n_chunks;
+    const int c0 = min(n_occ, c * per), c1 = min(n_occ, c0 + per);
     __shared__ float2 sq[kSpThreads];
     __shared__ int sx[kSpThreads], sy[kSpThreads], sz[kSpThreads];
     float2 acc[kSpMaxPerThread];
@@ -1062,7 +1069,7 @@ __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdA
     for (int k = 0; k < kSpMaxPerThread; ++k) acc[k] = make_float2(0.f, 0.f);
     const float2* pin = a.p_in + static_cast<int64_t>(s) * g.P;
     const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg;
-    for (int t0 = 0; t0 < n_occ; t0 += kSpThreads) {
+    for (int t0 = c0; t0 < c1; t0 += kSpThreads) {
         const int j = t0 + threadIdx.x;
         if (j < n_occ) {
             const int pt = a.idx[j];
@@ -1073,11 +1080,12 @@ __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdA
             sz[threadIdx.x] = rest / g.Ny;
         }
         __syncthreads();
-        const int nt = min(kSpThreads, n_occ - t0);
+        const int nt = min(kSpThreads, c1 - t0);
         for (int k = 0; k < kSpMaxPerThread; ++k) {
             const int e = threadIdx.x + k * kSpThreads;
             if (e >= g.E) break;
             const int ey = e / g.Ex, ex = e - ey * g.Ex;
+            float2 bacc = make_float2(0.f, 0.f);
             for (int i = 0; i < nt; ++i) {
                 const int ox = sx[i] + (g.Ex - 1 - ex) * g.ppx, oy = sy[i] + (g.Ey - 1 - ey) * g.ppy;
                 float2 h;
@@ -1085,38 +1093,54 @@ __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdA
                     h = gen_entry(a.gen, gen_row(a.gen, f, sz[i], oy), ox);
                 else
                     h = __ldg(a.table + ((static_cast<int64_t>(f) * g.Nz + sz[i]) * g.Noy + oy) * g.Nox + ox);
-                cmac(acc[k], h, sq[i]);
+                cmac(bacc, h, sq[i]);
             }
+            acc[k].x += bacc.x;
+            acc[k].y += bacc.y;
         }
         __syncthreads();
     }
+    const int64_t n = static_cast<int64_t>(gridDim.x) * a.B * g.E;
     for (int k = 0; k < kSpMaxPerThread; ++k) {
         const int e = threadIdx.x + k * kSpThreads;
-        if (e < g.E) a.G[(static_cast<int64_t>(s) * a.B + b) * g.E + e] = acc[k];
+        if (e < g.E) a.part[c * n + (static_cast<int64_t>(s) * a.B + b) * g.E + e] = acc[k];
     }
 }
 
-// the occupancy pass and the compacted forward; returns the choice word the dense kernels read
-cudaError_t launch_occupancy(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, const int** sel) {
+// the occupancy pass and the compacted forward; returns the choice word the dense kernels read and
+// the number of partials the compacted forward writes into the plan's partial-sum workspace
+cudaError_t launch_occupancy(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, const int** sel,
+                             int* sparse_groups) {
     *sel = nullptr;
+    *sparse_groups = 0;
     if (!p->occ_idx || p->E > kSpThreads * kSpMaxPerThread) return cudaSuccess;
-    const int64_t limit = p->occ_limit < 0 ? p->P / 16 : p->occ_limit;
+    // default limit: the compacted contraction gathers its table entries (stored) or generates them
+    // one by one (streamed, generated), so it pays off below N_points/16 or N_points/32 occupied points
+    const int64_t limit = p->occ_limit < 0 ? p->P / (p->table_mode == CUI_STORAGE_STORED ? 16 : 32) : p->occ_limit;
     if (limit == 0) return cudaSuccess;
+    // point chunks: about four blocks per SM over (slot, object, chunk), as many as the workspace holds
+    const int64_t per_group = static_cast<int64_t>(p->S) * B * p->E;
+    const int64_t fit = static_cast<int64_t>(p->ws_part_bytes / (sizeof(float2) * std::max<int64_t>(1, per_group)));
+    const int64_t want = (4 * 152 + static_cast<int64_t>(p->S) * B - 1) / (static_cast<int64_t>(p->S) * B);
+    const int chunks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({want, fit, 64})));
+    if (fit < 1) return cudaSuccess;
     occ_count_kernel<<<p->occ_nblk, kOccBlock, 0, st>>>(gamma, ldg, B, p->P, p->occ_cnt);
     occ_scan_kernel<<<1, 1024, 0, st>>>(p->occ_cnt, p->occ_nblk, limit);
     occ_scatter_kernel<<<p->occ_nblk, kOccBlock, 0, st>>>(gamma, ldg, B, p->P, p->occ_cnt, p->occ_nblk, p->occ_idx);
     SparseFwdArgs a;
     a.g = geom_of(p);
     a.table = p->table; a.gen = p->gen; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
-    a.slot_f = p->slot_f; a.idx = p->occ_idx; a.cnt = p->occ_cnt; a.nblk = p->occ_nblk; a.B = B; a.G = p->ws_G;
+    a.slot_f = p->slot_f; a.idx = p->occ_idx; a.cnt = p->occ_cnt; a.nblk = p->occ_nblk; a.B = B;
+    a.n_chunks = chunks; a.part = p->ws_part;
     // entries are generated where the table is not stored (the chunk buffer of a streamed plan is
     // refilled by the dense launch)
     if (p->table_mode == CUI_STORAGE_STORED)
-        sparse_fwd_kernel<false><<<dim3(p->S, B), kSpThreads, 0, st>>>(a);
+        sparse_fwd_kernel<false><<<dim3(p->S, B, chunks), kSpThreads, 0, st>>>(a);
     else
-        sparse_fwd_kernel<true><<<dim3(p->S, B), kSpThreads, 0, st>>>(a);
+        sparse_fwd_kernel<true><<<dim3(p->S, B, chunks), kSpThreads, 0, st>>>(a);
     count_launch(4);
     *sel = p->occ_cnt + 2 * p->occ_nblk + 1;
+    *sparse_groups = chunks;
     return cudaGetLastError();
 }
 
@@ -1140,12 +1164,13 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     if (p->precision == 2) return run_forward_phi(p, gamma, ldg, B, u, ldu, st);
     int groups = p->fwd_groups;
     const int* occ_sel = nullptr;
+    int sparse_groups = 0;
     if (p->precision == 1 && p->tc2) {
         e = launch_fwd_tc2(p, gamma, ldg, B, st, &groups);
     } else if (p->precision == 1) {
         e = launch_fwd_tc(p, gamma, ldg, B, st);
     } else {
-        if ((e = launch_occupancy(p, gamma, ldg, B, st, &occ_sel)) != cudaSuccess) return e;
+        if ((e = launch_occupancy(p, gamma, ldg, B, st, &occ_sel, &sparse_groups)) != cudaSuccess) return e;
         switch (pick_nc(p->max_slots_per_f)) {
             case 1: e = launch_fwd<1>(p, gamma, ldg, B, st, occ_sel); break;
             case 2: e = launch_fwd<2>(p, gamma, ldg, B, st, occ_sel); break;
@@ -1158,7 +1183,7 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     }
     if (e != cudaSuccess) return e;
     const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
-    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G, occ_sel);
+    reduce_groups_kernel<<<grid_1d(n, 256), 256, 0, st>>>(p->ws_part, groups, n, p->ws_G, occ_sel, sparse_groups);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (use_mix_tile(p, B)) {
