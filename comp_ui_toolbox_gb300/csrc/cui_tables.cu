@@ -8,10 +8,11 @@
 // incident fields (+scattering/+sequences/sequence.m:813-844) and the
 // prefactors (setup.m:759, sequence.m:623).  cui_born_plan_create_setup does
 // the same on the GPU:
-//   * the lateral-offset table in FP64 arithmetic (one thread per entry),
-//     stored in FP32; the 2D Green's function needs H0^(2) of a complex
-//     argument, evaluated here from its power series (DLMF 10.8.2) for
-//     |z| < 16 and from Hankel's asymptotic expansion (DLMF 10.17.4) above;
+//   * the lateral-offset table (one thread per entry), stored in FP32:
+//     distances and phases in FP64, the rest in FP32; the 2D Green's function
+//     needs H0^(2) of a complex argument, evaluated here from its power series
+//     (DLMF 10.8.2, FP64) for |z| < 16 and from Hankel's asymptotic expansion
+//     (DLMF 10.17.4, FP32 on the FP64-reduced phase) above;
 //   * the incident field of every (wave, frequency) as the sum over transmit
 //     elements of table rows shifted by the element offset, weighted by the
 //     normal velocities v_d;
@@ -104,11 +105,72 @@ __device__ double2 hankel2_0(double2 z) {
     return make_double2(J.x + Y.y, J.y - Y.x);  // J - i Y
 }
 
+// raised-cosine roll-off (raised_cosine.m:106-119); the cosine of the transition band in FP32
 __device__ inline double raised_cosine(double flag, double beta) {
     const double lb = kPi * (1.0 - beta);
     if (flag <= lb) return 1.0;
     if (flag >= kPi) return 0.0;
-    return 0.5 * (1.0 + cos(kPi * (flag - lb) / (kPi - lb)));
+    return 0.5 * (1.0 + static_cast<double>(cosf(static_cast<float>(kPi * (flag - lb) / (kPi - lb)))));
+}
+
+// ---- table entries: FP64 where FP32 cannot carry the accuracy, FP32 elsewhere ------------------
+// The table is stored in FP32.  Its entries need the distance D and the phase k~ D in FP64 (k~ D
+// reaches 10^3-10^4 rad); once the phase is reduced modulo 2 pi in FP64, its sine and cosine, the
+// attenuation, the prefactor and the asymptotic series of the Hankel function are FP32 work.
+// This GPU's FP64 rate is a small fraction of its FP32 rate, and the all-FP64 entry cost about a
+// thousand FP64 operations.
+constexpr double kTwoPi = 6.283185307179586476925;
+
+__device__ inline float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// principal square root, FP32
+__device__ inline float2 csqrtf_principal(float2 a) {
+    const float r = hypotf(a.x, a.y);
+    float re = sqrtf(0.5f * (r + fabsf(a.x)));
+    float im = (re > 0.f) ? 0.5f * a.y / re : 0.f;
+    if (a.x < 0.f) {
+        const float t = re;
+        re = fabsf(im);
+        im = copysignf(t, a.y);
+    }
+    return make_float2(re, im);
+}
+
+// exp(y) (cos x - i sin x) for a phase x of any size: x - n 2 pi with n = rint(x / 2 pi) by one FP64
+// FMA (its error, |n| times that of fl(2 pi), stays below 1e-11 rad for |x| < 1e5), then FP32 sine
+// and cosine of the reduced phase in [-pi, pi]
+__device__ inline float2 exp_minus_i_f32(double x, double y) {
+    const double n = rint(x * (1.0 / kTwoPi));
+    const float r = static_cast<float>(fma(-n, kTwoPi, x));
+    float sn, cs;
+    sincosf(r, &sn, &cs);
+    const float m = expf(static_cast<float>(y));
+    return make_float2(m * cs, -m * sn);
+}
+
+// H0^(2)(z) of a table entry: for |z| >= 16 Hankel's expansion (DLMF 10.17.4) in FP32 with the
+// phase reduced in FP64; nearer the array the FP64 power series of hankel2_0 (its terms cancel).
+__device__ inline double2 hankel2_0_entry(double2 z) {
+    if (z.x * z.x + z.y * z.y < kHankelSwitch * kHankelSwitch) return hankel2_0(z);
+    const float2 zf = make_float2(static_cast<float>(z.x), static_cast<float>(z.y));
+    const float d = zf.x * zf.x + zf.y * zf.y;
+    const float2 w = make_float2(zf.x / d, -zf.y / d);  // 1/z
+    float2 term = make_float2(1.f, 0.f), sum = term;
+    float prev = 1.f;  // squared magnitude of the last term
+    for (int k = 1; k < 32; ++k) {
+        const float c = (2.f * k - 1.f) * (2.f * k - 1.f) / (8.f * k);
+        const float2 next = cmulf(cmulf(term, make_float2(0.f, c)), w);  // * (-i) * (-(2k-1)^2/(8k)) / z
+        const float mag = next.x * next.x + next.y * next.y;
+        if (mag >= prev) break;  // truncated at the smallest term
+        term = next;
+        sum.x += term.x;
+        sum.y += term.y;
+        prev = mag;
+        if (mag < 1e-15f) break;  // below FP32 resolution of a sum close to 1
+    }
+    const float2 pre = csqrtf_principal(make_float2(w.x * static_cast<float>(2.0 / kPi), w.y * static_cast<float>(2.0 / kPi)));
+    const float2 r = cmulf(cmulf(pre, exp_minus_i_f32(z.x - 0.25 * kPi, z.y)), sum);
+    return make_double2(r.x, r.y);
 }
 
 struct TableArgs {
@@ -120,7 +182,8 @@ struct TableArgs {
     int* bad;           // set when an entry is not finite
 };
 
-// one thread per entry (f, z, oy, ox); FP64 arithmetic, FP32 store
+// one thread per entry (f, z, oy, ox); distances and phases in FP64, the rest in FP32 (see above),
+// FP32 store
 __global__ void table_kernel(const TableArgs a) {
     const int64_t n = static_cast<int64_t>(a.F) * a.Nz * a.Noy * a.Nox;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
@@ -144,10 +207,11 @@ __global__ void table_kernel(const TableArgs a) {
                 const double2 kD = cscale(k, D);
                 double2 G;
                 if (a.n_dims == 2) {
-                    const double2 h = hankel2_0(kD);
-                    G = make_double2(-0.25 * h.y, 0.25 * h.x);             // 0.25j * H0^(2)(kD)
-                } else {
-                    G = cscale(cexp_minus_i(kD), -1.0 / (4.0 * kPi * D));  // -exp(-j k D)/(4 pi D)
+                    const double2 h = hankel2_0_entry(kD);
+                    G = make_double2(-0.25 * h.y, 0.25 * h.x);  // 0.25j * H0^(2)(kD)
+                } else {                                         // -exp(-j k D)/(4 pi D)
+                    const float2 e = exp_minus_i_f32(kD.x, kD.y);
+                    G = cscale(make_double2(e.x, e.y), -1.0 / (4.0 * kPi * D));
                 }
                 if (a.w) G = cmul(G, a.w[(static_cast<int64_t>(f) * a.Qy + qy) * a.Qx + qx]);
                 sum = cadd(sum, G);

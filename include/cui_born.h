@@ -125,10 +125,11 @@ typedef struct {
 
 /* ---- setup form: tables built on the device ---------------------------------
  * Instead of the precomputed tables, the caller describes the discretised
- * setup; the plan computes the lateral transfer-function table (FP64
- * arithmetic, setup.m:1216-1281, greens_function.m:88/103, on.m:64-70,
- * raised_cosine.m:106-119), the incident fields (sequence.m:813-844) and the
- * prefactors -dV k~^2 R (setup.m:759, sequence.m:623) on the GPU. */
+ * setup; the plan computes the lateral transfer-function table (distances and
+ * phases in FP64, the rest in FP32; setup.m:1216-1281, greens_function.m:88/103,
+ * on.m:64-70, raised_cosine.m:106-119), the incident fields
+ * (sequence.m:813-844) and the prefactors -dV k~^2 R (setup.m:759,
+ * sequence.m:623) on the GPU. */
 typedef enum { CUI_ABSORPTION_NONE = 0, CUI_ABSORPTION_TIME_CAUSAL = 1 } cui_absorption_kind;
 
 typedef struct {
@@ -221,8 +222,8 @@ cui_status cui_born_setup_hash(const cui_born_setup_desc* desc, char* hex17);
  *     received-energy kernels compute each entry where they stage it.  No table
  *     memory (table_bytes 0), at about 1.5x the apply time of the other two.
  * Generated entries are formed in FP32 with the distance and the phase range
- * reduction in FP32 pairs (relative entry error below 1e-6; the stored table is
- * computed in FP64 and rounded to FP32).  Streamed and generated plans run the
+ * reduction in FP32 pairs (relative entry error below 1e-6; the stored table
+ * keeps distances and phases in FP64, the rest in FP32, entry error below 4e-7).  Streamed and generated plans run the
  * FP32 CUDA-core kernels only (cui_born_set_precision(BF16X3) is
  * CUI_ERR_UNSUPPORTED_SETUP); their received energies, the Phi columns of
  * cui_born_omp / cui_born_cosamp and cui_born_forward_static generate the
