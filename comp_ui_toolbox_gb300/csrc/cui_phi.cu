@@ -194,32 +194,44 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs a) {
 // per-apply operands: B forms of gamma (forward) and of u (adjoint)
 // ---------------------------------------------------------------------------
 // forms[k8][nb 32][c 2][8 n][8 k] bf16 with n = form * 64 + b; k runs over the 8 points
-// (gamma) or 8 rows (u) of K step k8.  Thread per 16-byte row piece (k8, n, c).
+// (gamma) or 8 rows (u) of K step k8.  A block takes 8 K steps (64 points or rows) at a time: it
+// stages the 64 objects x 64 entries of x in shared memory with coalesced loads (one object's 64
+// consecutive entries per pass of 64 threads), then writes the 8 x 512 pieces of 16 bytes, one
+// per (k8, n, c), each from 8 staged entries.
+constexpr int kFormsK8 = 8;  // K steps per block pass
 template <bool ADJ>
 __global__ void __launch_bounds__(256) forms_kernel(const float2* __restrict__ x, int64_t ldx, int B, int64_t n_in,
                                                     int64_t n_k8, uint4* __restrict__ out) {
-    const int64_t n = n_k8 * 512;
-    for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < n;
-         idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t k8 = idx >> 9;
-        const int w = static_cast<int>(idx & 511);
-        const int nrow = (w >> 4) * 8 + (w & 7), c = (w >> 3) & 1;
-        const int form = nrow >> 6, b = nrow & 63;
-        uint32_t v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int64_t i = k8 * 8 + k;
-            const float2 z = (b < B && i < n_in) ? x[static_cast<int64_t>(b) * ldx + i] : make_float2(0.f, 0.f);
-            float val;
-            if (!ADJ)  // gamma = g + ih: B1 = (g, -h), B2 = (h, g)
-                val = (form & 1) ? (c ? z.x : z.y) : (c ? -z.y : z.x);
-            else       // u = c + id: B1 = (c, d), B2 = (d, -c)
-                val = (form & 1) ? (c ? -z.x : z.y) : (c ? z.y : z.x);
-            uint32_t hi, lo;
-            split1(val, hi, lo);
-            v[k] = (form >= 2) ? lo : hi;
+    __shared__ float2 tile[kPhiObj][kFormsK8 * 8 + 1];  // [object][entry], padded against bank conflicts
+    for (int64_t blk = blockIdx.x; blk * kFormsK8 < n_k8; blk += gridDim.x) {
+        const int64_t k80 = blk * kFormsK8, i0 = k80 * 8;
+        for (int e = threadIdx.x; e < kPhiObj * kFormsK8 * 8; e += blockDim.x) {
+            const int b = e / (kFormsK8 * 8), kk = e % (kFormsK8 * 8);
+            const int64_t i = i0 + kk;
+            tile[b][kk] = (b < B && i < n_in) ? x[static_cast<int64_t>(b) * ldx + i] : make_float2(0.f, 0.f);
         }
-        out[idx] = pack8(v);
+        __syncthreads();
+        for (int e = threadIdx.x; e < kFormsK8 * 512; e += blockDim.x) {
+            const int k8l = e >> 9, w = e & 511;
+            if (k80 + k8l >= n_k8) break;
+            const int nrow = (w >> 4) * 8 + (w & 7), c = (w >> 3) & 1;
+            const int form = nrow >> 6, b = nrow & 63;
+            uint32_t v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float2 z = tile[b][k8l * 8 + k];
+                float val;
+                if (!ADJ)  // gamma = g + ih: B1 = (g, -h), B2 = (h, g)
+                    val = (form & 1) ? (c ? z.x : z.y) : (c ? -z.y : z.x);
+                else       // u = c + id: B1 = (c, d), B2 = (d, -c)
+                    val = (form & 1) ? (c ? -z.x : z.y) : (c ? z.y : z.x);
+                uint32_t hi, lo;
+                split1(val, hi, lo);
+                v[k] = (form >= 2) ? lo : hi;
+            }
+            out[(k80 + k8l) * 512 + w] = pack8(v);
+        }
+        __syncthreads();
     }
 }
 
@@ -703,7 +715,7 @@ cui_status phi_prepare(Plan& p) {
 // Forward GEMM of objects [0, B) (B <= 64): B forms of gamma, then partials
 // part[kc][b][row] of u; returns the chunk count the reduction adds.
 cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* n_kc) {
-    forms_kernel<false><<<grid_1d(p->phi_npb * 512, 256), 256, 0, st>>>(gamma, ldg, B, p->P, p->phi_npb,
+    forms_kernel<false><<<grid_1d((p->phi_npb + kFormsK8 - 1) / kFormsK8 * 256, 256), 256, 0, st>>>(gamma, ldg, B, p->P, p->phi_npb,
                                                                         reinterpret_cast<uint4*>(p->phi_gforms));
     count_launch();
     cudaError_t e = cudaGetLastError();
@@ -727,7 +739,7 @@ cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cud
 // Adjoint GEMM of objects [0, B) (B <= 64): B forms of u, then partials part[kc][b][point].
 cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc) {
     const int64_t nrb8 = p->phi_rows_pad / 8;
-    forms_kernel<true><<<grid_1d(nrb8 * 512, 256), 256, 0, st>>>(u, ldu, B, p->n_obs, nrb8,
+    forms_kernel<true><<<grid_1d((nrb8 + kFormsK8 - 1) / kFormsK8 * 256, 256), 256, 0, st>>>(u, ldu, B, p->n_obs, nrb8,
                                                                  reinterpret_cast<uint4*>(p->phi_uforms));
     count_launch();
     cudaError_t e = cudaGetLastError();
