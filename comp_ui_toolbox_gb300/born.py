@@ -404,7 +404,8 @@ class OperatorBorn:
 
     def set_occupancy_limit(self, max_points: int = -1) -> None:
         """FP32 forward: contract over the occupied points when there are at most ``max_points``
-        (``cui_born_set_occupancy_limit``; -1: N_points / 16, 0: always dense)."""
+        (``cui_born_set_occupancy_limit``; -1: N_points / 16 with a stored table, / 32 with a
+        streamed or generated one; 0: always dense)."""
         _check(self._lib.cui_born_set_occupancy_limit(self._plan, int(max_points)))
 
     def device_status(self) -> int:

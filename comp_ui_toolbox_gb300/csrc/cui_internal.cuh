@@ -101,7 +101,7 @@ struct Plan {
     int* occ_idx = nullptr;         // [P] occupied points, ascending
     int* occ_cnt = nullptr;         // [2 * occ_nblk + 2]: per-block counts, offsets, then n_occ and the choice
     int occ_nblk = 0;               // 1024-point blocks
-    int64_t occ_limit = -1;         // compact when n_occ <= occ_limit (-1: P / 16; 0: never)
+    int64_t occ_limit = -1;         // compact when n_occ <= occ_limit (-1: P / 16 stored, P / 32 otherwise; 0: never)
 
     // launch geometry chosen at creation
     int fwd_groups = 1;             // line groups of the dense forward

@@ -461,7 +461,8 @@ cui_status cui_born_set_wait_limit(cui_born_plan* plan, int64_t nanoseconds);
  * FP32 forward first lists those points on the device; when there are at most max_points of
  * them it contracts over the list (work proportional to their number), otherwise it runs the
  * dense kernels.  The choice is made on the device (no synchronisation).  max_points = -1
- * selects the default, N_points / 16; 0 turns the compaction off.  The split-BF16 paths
+ * selects the default, N_points / 16 with a stored table and N_points / 32 with
+ * a streamed or generated one; 0 turns the compaction off.  The split-BF16 paths
  * always contract densely. */
 cui_status cui_born_set_occupancy_limit(cui_born_plan* plan, int64_t max_points);
 /* Reads and clears the plan's device status word; CUI_ERR_TIMEOUT when a
