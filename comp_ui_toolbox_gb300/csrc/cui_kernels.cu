@@ -872,7 +872,6 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
                                                                           : fwd_dense_kernel<NC, KE>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    if ((e = timing_begin(const_cast<Plan*>(p), 0, st)) != cudaSuccess) return e;
     // streamed table: one chunk of frequencies at a time, generated into the chunk buffer and consumed
     // by the stored-table kernel before the next chunk overwrites it (stream order)
     const int fstep = p->table_mode == CUI_STORAGE_STREAMED ? p->stream_nf : p->F;
@@ -886,7 +885,7 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    return timing_end(const_cast<Plan*>(p), st);
+    return cudaSuccess;
 }
 
 template <int NC, int KJ>
@@ -1170,6 +1169,9 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
     } else if (p->precision == 1) {
         e = launch_fwd_tc(p, gamma, ldg, B, st);
     } else {
+        // the forward's timed region (cui_born_timing_*) covers the occupancy pass, the compacted
+        // contraction and the dense launches, whichever of the two contracts
+        if ((e = timing_begin(p, 0, st)) != cudaSuccess) return e;
         if ((e = launch_occupancy(p, gamma, ldg, B, st, &occ_sel, &sparse_groups)) != cudaSuccess) return e;
         switch (pick_nc(p->max_slots_per_f)) {
             case 1: e = launch_fwd<1>(p, gamma, ldg, B, st, occ_sel); break;
@@ -1180,6 +1182,7 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
             case 12: e = launch_fwd<12>(p, gamma, ldg, B, st, occ_sel); break;
             default: e = launch_fwd<16>(p, gamma, ldg, B, st, occ_sel); break;
         }
+        if (e == cudaSuccess) e = timing_end(p, st);
     }
     if (e != cudaSuccess) return e;
     const int64_t n = static_cast<int64_t>(p->S) * B * p->E;
