@@ -534,6 +534,10 @@ def run_ours(args):
     else:
         gamma = torch.randn((P, B), dtype=torch.float32, device="cuda", generator=gen).to(torch.complex64)
         gamma_kind = "seeded Gaussian (dense)"
+    # column-major storage (each column contiguous, the layout of MATLAB arrays and of the C-ABI), so
+    # that the Python wrapper hands the columns to the library without a transposing copy
+    gamma = gamma.t().contiguous().t()
+    u_meas = u_meas.t().contiguous().t()
     # union occupancy of the forward's columns: the reference's forward contracts only these points
     p_used = float((gamma.abs().amax(dim=1) > 0).float().mean())
     autotune = None

@@ -1037,7 +1037,10 @@ struct SparseFwdArgs {
     const float2* __restrict__ p_in;
     const float2* __restrict__ gamma;
     int64_t ldg;
-    const int* __restrict__ slot_f;
+    const int* __restrict__ f_slot_ptr;   // [F+1] slots of each frequency (CSR)
+    const int* __restrict__ f_slot_list;  // [S]
+    int n_sg;                          // slot groups per frequency (gridDim.x = F x n_sg)
+    int S;
     const int* __restrict__ idx;
     const int* __restrict__ cnt;       // n_occ at [2 nblk], the choice at [2 nblk + 1]
     int nblk, B;
@@ -1047,32 +1050,45 @@ struct SparseFwdArgs {
 
 constexpr int kSpThreads = 256;
 constexpr int kSpMaxPerThread = 4;  // elements per thread: arrays of up to 1024 elements
+constexpr int kSpSlots = 8;         // most slots of one frequency sharing each table entry
 
-// part[c][s][b][e] = sum over chunk c of the occupied points p of h(f_s; o(p, e), z_p) p_in[s][p]
-// gamma[b][p]: block per (slot, object, point chunk), thread per element (up to 4), the chunk's
-// points staged 256 at a time with their q = p_in gamma and grid coordinates.  Each staged batch
-// is summed on its own and then added to the chunk's total (two-level summation), and the chunks
-// are added in order by reduce_groups_kernel, so no accumulation chain runs over all points.
-template <bool GEN>
+// part[c][s][b][e] = sum over chunk c of the occupied points p of h(f; o(p, e), z_p) p_in[s][p]
+// gamma[b][p] for the slots s of frequency f: block per (frequency and group of up to 8 of its
+// slots, object, point chunk), thread per element (up to 4).  The chunk's points are staged 256
+// at a time with their grid coordinates and q = p_in gamma of every slot of the group; each table
+// entry is loaded (or generated) once per point and element and applied to all the group's slots.
+// Each staged batch is summed on its own and then added to the chunk's total (two-level
+// summation), and the chunks are added in order by reduce_groups_kernel, so no accumulation
+// chain runs over all points.
+template <bool GEN, int SG>
 __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdArgs a) {
     if (a.cnt[2 * a.nblk + 1] == 0) return;  // the dense kernels run instead
     const LineGeom& g = a.g;
-    const int s = blockIdx.x, b = blockIdx.y, c = blockIdx.z, f = a.slot_f[s];
+    const int f = blockIdx.x / a.n_sg, sg = blockIdx.x % a.n_sg;
+    const int b = blockIdx.y, c = blockIdx.z;
+    const int s_lo = a.f_slot_ptr[f] + sg * SG;
+    const int ns = min(SG, a.f_slot_ptr[f + 1] - s_lo);
+    if (ns <= 0) return;
     const int n_occ = a.cnt[2 * a.nblk];
     const int per = (n_occ + a.n_chunks - 1) / a.n_chunks;
     const int c0 = min(n_occ, c * per), c1 = min(n_occ, c0 + per);
-    __shared__ float2 sq[kSpThreads];
+    __shared__ float2 sq[SG][kSpThreads];
     __shared__ int sx[kSpThreads], sy[kSpThreads], sz[kSpThreads];
-    float2 acc[kSpMaxPerThread];
+    __shared__ int slots[SG];
+    if (threadIdx.x < SG) slots[threadIdx.x] = threadIdx.x < ns ? a.f_slot_list[s_lo + threadIdx.x] : 0;
+    __syncthreads();
+    float2 acc[kSpMaxPerThread][SG];
 #pragma unroll
-    for (int k = 0; k < kSpMaxPerThread; ++k) acc[k] = make_float2(0.f, 0.f);
-    const float2* pin = a.p_in + static_cast<int64_t>(s) * g.P;
+    for (int k = 0; k < kSpMaxPerThread; ++k)
+#pragma unroll
+        for (int j = 0; j < SG; ++j) acc[k][j] = make_float2(0.f, 0.f);
     const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg;
     for (int t0 = c0; t0 < c1; t0 += kSpThreads) {
-        const int j = t0 + threadIdx.x;
-        if (j < n_occ) {
-            const int pt = a.idx[j];
-            sq[threadIdx.x] = cmul(pin[pt], gam[pt]);
+        const int t = t0 + threadIdx.x;
+        if (t < c1) {
+            const int pt = a.idx[t];
+            const float2 gv = gam[pt];
+            for (int j = 0; j < ns; ++j) sq[j][threadIdx.x] = cmul(a.p_in[static_cast<int64_t>(slots[j]) * g.P + pt], gv);
             const int x = pt % g.Nx, rest = pt / g.Nx;
             sx[threadIdx.x] = x;
             sy[threadIdx.x] = rest % g.Ny;
@@ -1080,11 +1096,14 @@ __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdA
         }
         __syncthreads();
         const int nt = min(kSpThreads, c1 - t0);
+#pragma unroll
         for (int k = 0; k < kSpMaxPerThread; ++k) {
             const int e = threadIdx.x + k * kSpThreads;
             if (e >= g.E) break;
             const int ey = e / g.Ex, ex = e - ey * g.Ex;
-            float2 bacc = make_float2(0.f, 0.f);
+            float2 bacc[SG];
+#pragma unroll
+            for (int j = 0; j < SG; ++j) bacc[j] = make_float2(0.f, 0.f);
             for (int i = 0; i < nt; ++i) {
                 const int ox = sx[i] + (g.Ex - 1 - ex) * g.ppx, oy = sy[i] + (g.Ey - 1 - ey) * g.ppy;
                 float2 h;
@@ -1092,18 +1111,35 @@ __global__ void __launch_bounds__(kSpThreads) sparse_fwd_kernel(const SparseFwdA
                     h = gen_entry(a.gen, gen_row(a.gen, f, sz[i], oy), ox);
                 else
                     h = __ldg(a.table + ((static_cast<int64_t>(f) * g.Nz + sz[i]) * g.Noy + oy) * g.Nox + ox);
-                cmac(bacc, h, sq[i]);
+#pragma unroll
+                for (int j = 0; j < SG; ++j)
+                    if (j < ns) cmac(bacc[j], h, sq[j][i]);
             }
-            acc[k].x += bacc.x;
-            acc[k].y += bacc.y;
+#pragma unroll
+            for (int j = 0; j < SG; ++j) {
+                acc[k][j].x += bacc[j].x;
+                acc[k][j].y += bacc[j].y;
+            }
         }
         __syncthreads();
     }
-    const int64_t n = static_cast<int64_t>(gridDim.x) * a.B * g.E;
+    const int64_t n = static_cast<int64_t>(a.S) * a.B * g.E;
+#pragma unroll
     for (int k = 0; k < kSpMaxPerThread; ++k) {
         const int e = threadIdx.x + k * kSpThreads;
-        if (e < g.E) a.part[c * n + (static_cast<int64_t>(s) * a.B + b) * g.E + e] = acc[k];
+        if (e >= g.E) break;
+#pragma unroll
+        for (int j = 0; j < SG; ++j)
+            if (j < ns) a.part[c * n + (static_cast<int64_t>(slots[j]) * a.B + b) * g.E + e] = acc[k][j];
     }
+}
+
+template <int SG>
+void launch_sparse_fwd(bool gen, dim3 grid, const SparseFwdArgs& a, cudaStream_t st) {
+    if (gen)
+        sparse_fwd_kernel<true, SG><<<grid, kSpThreads, 0, st>>>(a);
+    else
+        sparse_fwd_kernel<false, SG><<<grid, kSpThreads, 0, st>>>(a);
 }
 
 // the occupancy pass and the compacted forward; returns the choice word the dense kernels read and
@@ -1117,10 +1153,26 @@ cudaError_t launch_occupancy(Plan* p, const float2* gamma, int64_t ldg, int B, c
     // one by one (streamed, generated), so it pays off below N_points/16 or N_points/32 occupied points
     const int64_t limit = p->occ_limit < 0 ? p->P / (p->table_mode == CUI_STORAGE_STORED ? 16 : 32) : p->occ_limit;
     if (limit == 0) return cudaSuccess;
-    // point chunks: about four blocks per SM over (slot, object, chunk), as many as the workspace holds
+    // point chunks: about four blocks per SM over (frequency and slot group, object, chunk), as many
+    // as the workspace holds
+    // slots per group, from {1, 2, 4, 8}: per (point, element) each group loads (about 16
+    // instructions) or generates (about 220, cui_gen.cuh) the table entry once and spends about 4 on
+    // each of its slots, padding included; the cheapest size wins, ties to the smaller (fewer registers)
+    const int ms = std::max(1, p->max_slots_per_f);
+    const int entry_cost = p->table_mode == CUI_STORAGE_STORED ? 16 : 220;
+    int sgz = 1, best = ms * (entry_cost + 4);
+    for (int cand = 2; cand <= kSpSlots; cand *= 2) {
+        const int cost = (ms + cand - 1) / cand * (entry_cost + 4 * cand);
+        if (cost < best) {
+            best = cost;
+            sgz = cand;
+        }
+    }
+    const int n_sg = (ms + sgz - 1) / sgz;
+    const int64_t fsg = static_cast<int64_t>(p->F) * n_sg * B;
     const int64_t per_group = static_cast<int64_t>(p->S) * B * p->E;
     const int64_t fit = static_cast<int64_t>(p->ws_part_bytes / (sizeof(float2) * std::max<int64_t>(1, per_group)));
-    const int64_t want = (4 * 152 + static_cast<int64_t>(p->S) * B - 1) / (static_cast<int64_t>(p->S) * B);
+    const int64_t want = (4 * 152 + fsg - 1) / fsg;
     const int chunks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({want, fit, 64})));
     if (fit < 1) return cudaSuccess;
     occ_count_kernel<<<p->occ_nblk, kOccBlock, 0, st>>>(gamma, ldg, B, p->P, p->occ_cnt);
@@ -1129,14 +1181,19 @@ cudaError_t launch_occupancy(Plan* p, const float2* gamma, int64_t ldg, int B, c
     SparseFwdArgs a;
     a.g = geom_of(p);
     a.table = p->table; a.gen = p->gen; a.p_in = p->p_in; a.gamma = gamma; a.ldg = ldg;
-    a.slot_f = p->slot_f; a.idx = p->occ_idx; a.cnt = p->occ_cnt; a.nblk = p->occ_nblk; a.B = B;
+    a.f_slot_ptr = p->f_slot_ptr; a.f_slot_list = p->f_slot_list; a.n_sg = n_sg; a.S = p->S;
+    a.idx = p->occ_idx; a.cnt = p->occ_cnt; a.nblk = p->occ_nblk; a.B = B;
     a.n_chunks = chunks; a.part = p->ws_part;
     // entries are generated where the table is not stored (the chunk buffer of a streamed plan is
     // refilled by the dense launch)
-    if (p->table_mode == CUI_STORAGE_STORED)
-        sparse_fwd_kernel<false><<<dim3(p->S, B, chunks), kSpThreads, 0, st>>>(a);
-    else
-        sparse_fwd_kernel<true><<<dim3(p->S, B, chunks), kSpThreads, 0, st>>>(a);
+    const dim3 grid(static_cast<unsigned>(p->F * n_sg), B, chunks);
+    const bool gen = p->table_mode != CUI_STORAGE_STORED;
+    switch (sgz) {
+        case 1: launch_sparse_fwd<1>(gen, grid, a, st); break;
+        case 2: launch_sparse_fwd<2>(gen, grid, a, st); break;
+        case 4: launch_sparse_fwd<4>(gen, grid, a, st); break;
+        default: launch_sparse_fwd<kSpSlots>(gen, grid, a, st); break;
+    }
     count_launch(4);
     *sel = p->occ_cnt + 2 * p->occ_nblk + 1;
     *sparse_groups = chunks;
