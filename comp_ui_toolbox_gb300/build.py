@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
             if verbose and out.strip():
                 print(out, file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    _run([cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
+    _run([cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread", "-ldl"])
     os.replace(tmp, LIB)
     build_harness()
     return LIB

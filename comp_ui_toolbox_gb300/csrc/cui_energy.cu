@@ -140,6 +140,7 @@ __global__ void energy_reduce_kernel(const float* __restrict__ part, int chunks,
 }  // namespace cui
 
 extern "C" cui_status cui_born_energy_rx(cui_born_plan* plan, float* energy, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_energy_rx");
     using namespace cui;
     if (!plan || !energy) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
     Plan& p = plan->p;

@@ -410,6 +410,7 @@ struct OmpWork {
 extern "C" cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, int32_t n_atoms_max, float rel_rmse,
                                    int64_t* atoms, cui_complex32* coefficients, float* rel_residuals,
                                    int32_t* n_atoms, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_omp");
     using namespace cui;
     if (!plan || !y || !atoms || !coefficients || !n_atoms) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
     Plan& p = plan->p;
@@ -551,6 +552,7 @@ extern "C" cui_status cui_born_omp(cui_born_plan* plan, const cui_complex32* y, 
 extern "C" cui_status cui_born_cosamp(cui_born_plan* plan, const cui_complex32* y, int32_t sparsity, int32_t n_iter_max,
                                       float rel_rmse, int64_t* atoms, cui_complex32* coefficients,
                                       float* rel_residuals, int32_t* n_iter, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_cosamp");
     using namespace cui;
     if (!plan || !y || !atoms || !coefficients || !n_iter) return set_error(CUI_ERR_INVALID_ARG, "NULL argument");
     *n_iter = 0;

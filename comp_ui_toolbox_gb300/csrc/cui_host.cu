@@ -169,6 +169,7 @@ extern "C" {
 
 cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_complex64* input, int64_t ld_in,
                                   int32_t n_objects, cui_complex64* output, int64_t ld_out) {
+    const cui::NvtxRange nvtx_range("cui_born_combined_host");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     Plan& p = plan->p;
@@ -218,6 +219,7 @@ cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_c
 cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, int64_t ld_gamma,
                              const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects, cui_complex64* grad,
                              int64_t ld_grad, double* loss) {
+    const cui::NvtxRange nvtx_range("cui_born_vjp_host");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     Plan& p = plan->p;
@@ -279,6 +281,7 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
 extern "C" cui_status cui_born_lasso_host(cui_born_plan* plan, const cui_complex64* u_meas, int64_t ld_u,
                                           int32_t n_objects, cui_complex64* gamma, int64_t ld_gamma,
                                           const float* lambda, float step, int32_t n_iter) {
+    const cui::NvtxRange nvtx_range("cui_born_lasso_host");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     Plan& p = plan->p;

@@ -1528,6 +1528,7 @@ cudaError_t launch_fwd_static(const Plan* p, const float2* gamma, int64_t ldg, i
 
 extern "C" cui_status cui_born_forward_static(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma,
                                               int32_t n_objects, cui_complex32* u, int64_t ld_u, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_forward_static");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     Plan* p = &plan->p;

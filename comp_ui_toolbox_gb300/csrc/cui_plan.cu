@@ -584,6 +584,7 @@ using cui::set_error;
 extern "C" {
 
 cui_status cui_born_plan_create(const cui_born_desc* desc, int32_t max_objects, cui_born_plan** plan) {
+    const cui::NvtxRange nvtx_range("cui_born_plan_create");
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     *plan = nullptr;
     cui_born_plan* h = new (std::nothrow) cui_born_plan();
@@ -640,6 +641,7 @@ cui_status cui_born_size(const cui_born_plan* plan, int64_t* n_observations, int
 
 cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma, int32_t n_objects,
                             cui_complex32* u, int64_t ld_u, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_forward");
     cui_status s = cui::check_apply(plan, gamma, ld_gamma, plan ? plan->p.P : 0, n_objects, u, ld_u,
                                     plan ? plan->p.n_obs : 0);
     if (s != CUI_OK) return s;
@@ -650,6 +652,7 @@ cui_status cui_born_forward(cui_born_plan* plan, const cui_complex32* gamma, int
 
 cui_status cui_born_adjoint(cui_born_plan* plan, const cui_complex32* u, int64_t ld_u, int32_t n_objects,
                             cui_complex32* gamma_hat, int64_t ld_gamma, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_adjoint");
     cui_status s = cui::check_apply(plan, u, ld_u, plan ? plan->p.n_obs : 0, n_objects, gamma_hat, ld_gamma,
                                     plan ? plan->p.P : 0);
     if (s != CUI_OK) return s;
@@ -660,6 +663,7 @@ cui_status cui_born_adjoint(cui_born_plan* plan, const cui_complex32* u, int64_t
 
 cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t ld_gamma, const cui_complex32* u_meas,
                         int64_t ld_u, int32_t n_objects, cui_complex32* grad, int64_t ld_grad, float* loss, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_vjp");
     cui_status s = cui::check_apply(plan, gamma, ld_gamma, plan ? plan->p.P : 0, n_objects, grad, ld_grad,
                                     plan ? plan->p.P : 0);
     if (s != CUI_OK) return s;
@@ -673,6 +677,7 @@ cui_status cui_born_vjp(cui_born_plan* plan, const cui_complex32* gamma, int64_t
 cui_status cui_born_lasso(cui_born_plan* plan, const cui_complex32* u_meas, int64_t ld_u, int32_t n_objects,
                           cui_complex32* gamma, int64_t ld_gamma, const float* lambda, float step, int32_t n_iter,
                           float* loss, void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_lasso");
     cui_status s = cui::check_apply(plan, gamma, ld_gamma, plan ? plan->p.P : 0, n_objects, gamma, ld_gamma,
                                     plan ? plan->p.P : 0);
     if (s != CUI_OK) return s;

@@ -711,6 +711,7 @@ cui_status create_setup_plan(const cui_born_setup_desc* desc, int32_t max_object
 
 extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc, int32_t max_objects,
                                                  cui_born_plan** plan) {
+    const cui::NvtxRange nvtx_range("cui_born_plan_create_setup");
     const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return
     return create_setup_plan(desc, max_objects, CUI_STORAGE_AUTO, nullptr, nullptr, plan);
 }
@@ -718,6 +719,7 @@ extern "C" cui_status cui_born_plan_create_setup(const cui_born_setup_desc* desc
 extern "C" cui_status cui_born_plan_create_setup_ex(const cui_born_setup_desc* desc, int32_t max_objects,
                                                     int32_t storage, const char* cache_dir, cui_born_plan** plan,
                                                     int32_t* loaded) {
+    const cui::NvtxRange nvtx_range("cui_born_plan_create_setup_ex");
     if (loaded) *loaded = 0;
     const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return
     return create_setup_plan(desc, max_objects, storage, cache_dir, loaded, plan);
@@ -731,6 +733,7 @@ extern "C" cui_status cui_born_plan_table_storage(const cui_born_plan* plan, int
 
 extern "C" cui_status cui_born_plan_create_setup_cached(const cui_born_setup_desc* desc, int32_t max_objects,
                                                         const char* cache_dir, cui_born_plan** plan, int32_t* loaded) {
+    const cui::NvtxRange nvtx_range("cui_born_plan_create_setup_cached");
     if (!cache_dir) return cui::set_error(CUI_ERR_INVALID_ARG, "cache_dir is NULL");
     if (loaded) *loaded = 0;
     const cui::DeviceGuard restore(-1);  // the caller's current device is restored on return

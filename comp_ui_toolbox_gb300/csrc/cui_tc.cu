@@ -596,6 +596,7 @@ cui_status tc_prepare(Plan& p) {
 }  // namespace cui
 
 extern "C" cui_status cui_born_set_precision(cui_born_plan* plan, int32_t precision) {
+    const cui::NvtxRange nvtx_range("cui_born_set_precision");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     if (precision == CUI_PRECISION_FP32) {

@@ -58,6 +58,7 @@ cui_status time_path(Plan* p, const float2* g, float2* u, float2* gh, int B, cud
 
 extern "C" cui_status cui_born_autotune(cui_born_plan* plan, int32_t n_objects, int32_t* precision, double* ms,
                                         void* stream) {
+    const cui::NvtxRange nvtx_range("cui_born_autotune");
     using namespace cui;
     if (!plan) return set_error(CUI_ERR_INVALID_ARG, "plan is NULL");
     Plan& p = plan->p;
