@@ -191,11 +191,15 @@ cui_status cui_born_combined_host(cui_born_plan* plan, int32_t mode, const cui_c
         host_in_kernel<<<host_grid(rows_in, n_objects), 256>>>(input, ld_in, rows_in, p.d_stage_in);
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
+        bool written = false;  // the folded adjoint may write the caller's array itself
         s = (mode == 1) ? forward_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0)
-                        : adjoint_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0);
+                        : adjoint_device(&p, p.d_stage_in, rows_in, n_objects, p.d_stage_out, rows_out, 0,
+                                         HostOut{output, ld_out, &written});
         if (s != CUI_OK) return s;
-        launch_host_out(p.d_stage_out, rows_out, n_objects, output, ld_out);
-        count_launch();
+        if (!written) {
+            launch_host_out(p.d_stage_out, rows_out, n_objects, output, ld_out);
+            count_launch();
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host output");
         return check_cuda(cudaStreamSynchronize(0), "synchronize");
     }
@@ -238,10 +242,14 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
         host_in_kernel<<<host_grid(p.n_obs, n_objects), 256>>>(u_meas, ld_u, p.n_obs, p.d_stage_aux);
         count_launch(2);
         if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
-        s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0);
+        bool written = false;  // the folded adjoint may write the caller's gradient itself
+        s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0,
+                       HostOut{grad, ld_grad, &written});
         if (s != CUI_OK) return s;
-        launch_host_out(p.d_stage_out, p.P, n_objects, grad, ld_grad);
-        count_launch();
+        if (!written) {
+            launch_host_out(p.d_stage_out, p.P, n_objects, grad, ld_grad);
+            count_launch();
+        }
         if (loss) {
             host_loss_kernel<<<1, 128>>>(p.d_stage_loss, n_objects, loss);
             count_launch();

@@ -246,13 +246,20 @@ cui_status cache_store(const std::string& path, const std::vector<unsigned char>
 // apply entry points used by the host wrappers ----------------------------
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu,
                           cudaStream_t st);
+// With `host` (FP64 host columns, leading dimension ld_host) the folded path may write the result
+// there itself; *host_written then says it did (else the result is in g as usual).
+struct HostOut {
+    cui_complex64* host = nullptr;
+    int64_t ld = 0;
+    bool* written = nullptr;
+};
 cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg,
-                          cudaStream_t st);
+                          cudaStream_t st, HostOut ho = HostOut{});
 // n_iter proximal-gradient LASSO iterations, gamma updated in place (no allocation, no synchronisation)
 cui_status lasso_device(Plan* p, float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B, float step,
                         const float* lambda, int n_iter, float* loss, cudaStream_t st);
 cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
-                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st);
+                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho = HostOut{});
 
 // shared-memory bytes the contraction kernels request
 size_t fwd_smem_bytes(const Plan* p, int nc);
@@ -278,7 +285,8 @@ size_t phi_matrix_bytes(const Plan* p);
 bool phi_supported(const Plan* p, std::string* why);
 cui_status phi_prepare(Plan& p);
 cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cudaStream_t st, int* n_kc);
-cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc);
+cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc,
+                           cui_complex64* host = nullptr, int64_t ld_host = 0);
 
 // timing hooks around a contraction launch (no-ops unless timing is enabled)
 cudaError_t timing_begin(Plan* p, int kind, cudaStream_t st);

@@ -1288,12 +1288,16 @@ cudaError_t finish_adjoint(Plan* p, const float2* part, int nfc, int B, float2* 
 // adjoint against the folded operator: 64-object GEMM passes straight from the observations
 // (no unmixing: the mixes are inside the matrix)
 cudaError_t run_adjoint_phi(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
-                            const IstaArgs* ista) {
+                            const IstaArgs* ista, HostOut ho = HostOut{}) {
+    if (ho.written) *ho.written = ho.host != nullptr && !ista;
     for (int b0 = 0; b0 < B; b0 += 64) {
         const int nb = std::min(64, B - b0);
         int nkc = 1;
-        cudaError_t e = launch_adj_phi(p, u + static_cast<int64_t>(b0) * ldu, ldu, nb, st, &nkc);
+        cudaError_t e = launch_adj_phi(p, u + static_cast<int64_t>(b0) * ldu, ldu, nb, st, &nkc,
+                                       (ho.host && !ista) ? ho.host + static_cast<int64_t>(b0) * ho.ld : nullptr, ho.ld);
         if (e != cudaSuccess) return e;
+        if (nkc == 0) continue;  // the GEMM wrote this pass's gradient to the host itself
+        if (ho.written) *ho.written = false;
         IstaArgs is{};
         if (ista) is = IstaArgs{ista->step, ista->lambda + b0};
         if ((e = finish_adjoint(p, p->phi_part, nkc, nb, g + static_cast<int64_t>(b0) * ldg, ldg, ista ? &is : nullptr,
@@ -1304,9 +1308,10 @@ cudaError_t run_adjoint_phi(Plan* p, const float2* u, int64_t ldu, int B, float2
 }
 
 cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
-                        const IstaArgs* ista = nullptr) {
+                        const IstaArgs* ista = nullptr, HostOut ho = HostOut{}) {
     cudaError_t e;
-    if (p->precision == 2) return run_adjoint_phi(p, u, ldu, B, g, ldg, st, ista);
+    if (ho.written) *ho.written = false;
+    if (p->precision == 2) return run_adjoint_phi(p, u, ldu, B, g, ldg, st, ista, ho);
     if (use_mix_tile(p, B)) {
         MixTileArgs t = mix_tile_args(p, B);
         t.uin = u; t.ldu = ldu; t.V = p->ws_G;
@@ -1402,12 +1407,13 @@ cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, floa
     return check_cuda(run_forward(p, gamma, ldg, B, u, ldu, st), "forward");
 }
 
-cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st) {
-    return check_cuda(run_adjoint(p, u, ldu, B, g, ldg, st), "adjoint");
+cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* g, int64_t ldg, cudaStream_t st,
+                          HostOut ho) {
+    return check_cuda(run_adjoint(p, u, ldu, B, g, ldg, st, nullptr, ho), "adjoint");
 }
 
 cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
-                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st) {
+                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho) {
     cudaError_t e = run_forward(p, gamma, ldg, B, p->ws_r, p->n_obs, st);
     if (e != cudaSuccess) return check_cuda(e, "vjp forward");
     residual_kernel<<<dim3(kLossBlocks, B), 256, 0, st>>>(p->ws_r, p->n_obs, um, ldu, p->n_obs, p->ws_loss);
@@ -1418,7 +1424,7 @@ cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* u
         count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "vjp loss");
     }
-    return check_cuda(run_adjoint(p, p->ws_r, p->n_obs, B, grad, ldgr, st), "vjp adjoint");
+    return check_cuda(run_adjoint(p, p->ws_r, p->n_obs, B, grad, ldgr, st, nullptr, ho), "vjp adjoint");
 }
 
 cui_status lasso_device(Plan* p, float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B, float step,

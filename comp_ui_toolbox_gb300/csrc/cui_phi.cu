@@ -247,6 +247,8 @@ struct PhiGemmArgs {
     int B;                  // objects of this pass (<= 64)
     int64_t n_out;          // valid output rows (forward: observations) or points (adjoint)
     float2* part;           // [n_kc][B][n_out]
+    double2* host_out;      // adjoint with one K chunk: the caller's FP64 host columns (16-byte aligned,
+    int64_t host_ld;        // leading dimension host_ld), written instead of part; else nullptr
     int* status;
     uint64_t wait_ns;
 };
@@ -406,7 +408,14 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
         }
         if (ok && nch > 0) {
             const int64_t row = tile * 256 + t * 128 + qd * 32 + lane;
-            if (row < a.n_out) {
+            if (row < a.n_out && ADJ && a.host_out) {
+                // the finished gradient straight into the caller's host array (through the host page
+                // tables), with streaming stores: 32 lanes write 512 contiguous bytes per object
+                double2* out = a.host_out + row;
+#pragma unroll
+                for (int b = 0; b < 64; ++b)
+                    if (b < a.B) __stcs(out + static_cast<int64_t>(b) * a.host_ld, make_double2(acc[b], acc[64 + b]));
+            } else if (row < a.n_out) {
                 float2* out = a.part + static_cast<int64_t>(kc) * a.B * a.n_out + row;
 #pragma unroll
                 for (int b = 0; b < 64; ++b)
@@ -723,6 +732,7 @@ cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cud
     PhiGemmArgs a;
     a.phi = p->phi; a.bf = p->phi_gforms; a.npb = p->phi_npb; a.nrb8 = p->phi_rows_pad / 8; a.n_kc = p->phi_fwd_kc;
     a.B = B; a.n_out = p->n_obs; a.part = p->phi_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
+    a.host_out = nullptr; a.host_ld = 0;
     if ((e = timing_begin(p, 0, st)) != cudaSuccess) return e;
     CUtensorMap unused;  // the forward's stages are contiguous runs (plain bulk copies)
     std::memset(&unused, 0, sizeof unused);
@@ -736,8 +746,11 @@ cudaError_t launch_fwd_phi(Plan* p, const float2* gamma, int64_t ldg, int B, cud
     return cudaSuccess;
 }
 
-// Adjoint GEMM of objects [0, B) (B <= 64): B forms of u, then partials part[kc][b][point].
-cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc) {
+// Adjoint GEMM of objects [0, B) (B <= 64): B forms of u, then partials part[kc][b][point].  With
+// `host` (16-byte aligned FP64 columns, leading dimension ld_host) and one K chunk the GEMM writes
+// the gradient there itself and *n_kc is 0: nothing is left to reduce.
+cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStream_t st, int* n_kc,
+                           cui_complex64* host, int64_t ld_host) {
     const int64_t nrb8 = p->phi_rows_pad / 8;
     forms_kernel<true><<<grid_1d((nrb8 + kFormsK8 - 1) / kFormsK8 * 256, 256), 256, 0, st>>>(u, ldu, B, p->n_obs, nrb8,
                                                                  reinterpret_cast<uint4*>(p->phi_uforms));
@@ -747,6 +760,9 @@ cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStr
     PhiGemmArgs a;
     a.phi = p->phi; a.bf = p->phi_uforms; a.npb = p->phi_npb; a.nrb8 = nrb8; a.n_kc = p->phi_adj_kc;
     a.B = B; a.n_out = p->P; a.part = p->phi_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
+    const bool to_host = host != nullptr && p->phi_adj_kc == 1 && (reinterpret_cast<uintptr_t>(host) & 15) == 0;
+    a.host_out = to_host ? reinterpret_cast<double2*>(host) : nullptr;
+    a.host_ld = ld_host;
     if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
     CUtensorMap tmap;
     std::memcpy(&tmap, p->phi_tmap, sizeof tmap);
@@ -756,7 +772,7 @@ cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStr
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = timing_end(p, st)) != cudaSuccess) return e;
-    *n_kc = p->phi_adj_kc;
+    *n_kc = to_host ? 0 : p->phi_adj_kc;
     return cudaSuccess;
 }
 

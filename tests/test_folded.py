@@ -123,3 +123,34 @@ def test_folded_refused_without_stored_table():
         op.set_precision("bf16x3-folded")
     assert ei.value.status == 2
     op.close()
+
+
+def test_folded_host_vjp_writes_the_callers_array():
+    """On a full 512 x 512 grid each adjoint block covers all rows (one K chunk), so in the direct
+    host path the GEMM writes the FP64 gradient into the caller's array itself.  It equals the
+    device VJP's gradient exactly (the same FP32 values, converted to FP64), for an aligned output
+    and for one 8 bytes off a 16-byte boundary, which takes the separate write-back instead."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload("2d-batched")
+    w.f = w.f[:2]
+    B = 8
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=B)
+    op.set_precision("bf16x3-folded")
+    rng = np.random.default_rng(12)
+    g = np.asfortranarray((rng.standard_normal((op.n_points, B)) + 1j * rng.standard_normal((op.n_points, B))).astype(np.complex64).astype(np.complex128))
+    u = np.asfortranarray((rng.standard_normal((op.n_observations, B)) + 1j * rng.standard_normal((op.n_observations, B))).astype(np.complex64).astype(np.complex128))
+    grad_d, loss_d = op.vjp(dev(g), dev(u))
+    grad_d = grad_d.cpu().numpy().astype(np.complex128)
+    grad_h, loss_h = op.vjp(g, u)
+    assert np.array_equal(grad_h, grad_d)
+    np.testing.assert_allclose(loss_h, loss_d.cpu().numpy(), rtol=1e-6)
+    nbytes = g.size * 16
+    raw = np.zeros(nbytes + 32, dtype=np.uint8)
+    off = (8 - raw.ctypes.data % 16) % 16
+    out = raw[off:off + nbytes].view(np.complex128).reshape(g.shape, order="F")
+    op.vjp(g, u, out=out)
+    assert np.array_equal(out, grad_d)
+    assert op.device_status() == 0
+    op.close()
