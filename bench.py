@@ -607,6 +607,9 @@ def run_ours(args):
            "h2d_bytes_per_step": 16 * (P + N) * B, "d2h_bytes_per_step": 16 * P * B + 8 * B,
            "path": ("cui_born_vjp_host: the caller's FP64 host arrays read and written by device kernels through "
                     "the host page tables (Grace ATS over NVLink-C2C), VJP on the device in between"
+                    + ("; the folded adjoint GEMM writes the FP64 gradient into the caller's array itself (one K "
+                       "chunk per block)" if args.precision == "bf16x3-folded" and -(-P // 256) >= 4 * 152
+                       else "")
                     if host_path == "direct" else
                     "cui_born_vjp_host: FP64 host buffers -> FP32 pinned staging -> H2D -> VJP -> D2H -> FP64"),
            "bytes": "FP64 complex host data crossing host<->device per step (gamma and u in, gradient and loss out)"}

@@ -259,7 +259,9 @@ __device__ __forceinline__ bool wait_warp(uint32_t bar, uint32_t parity, volatil
 
 // ADJ = false: block (kc, row block RB) contracts its 256 rows over the point range of chunk kc.
 // ADJ = true: block (point block PS, kc) contracts its 256 points over the row range of chunk kc.
-template <bool ADJ, int KS, int NS>
+// HOST (adjoint with one K chunk): the epilogue writes the caller's FP64 host columns instead of
+// the partials; a separate instantiation, so the device-resident kernel carries no branch for it
+template <bool ADJ, int KS, int NS, bool HOST = false>
 __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmArgs a,
                                                                   const __grid_constant__ CUtensorMap tmap) {
     using C = PhiCfg<KS, NS>;
@@ -408,14 +410,21 @@ __global__ void __launch_bounds__(kPhiThreads, 1) phi_gemm_kernel(const PhiGemmA
         }
         if (ok && nch > 0) {
             const int64_t row = tile * 256 + t * 128 + qd * 32 + lane;
-            if (row < a.n_out && ADJ && a.host_out) {
+            if (HOST && row < a.n_out) {
                 // the finished gradient straight into the caller's host array (through the host page
                 // tables), with streaming stores: 32 lanes write 512 contiguous bytes per object
                 double2* out = a.host_out + row;
+                const int64_t ld = a.host_ld;
 #pragma unroll
-                for (int b = 0; b < 64; ++b)
-                    if (b < a.B) __stcs(out + static_cast<int64_t>(b) * a.host_ld, make_double2(acc[b], acc[64 + b]));
-            } else if (row < a.n_out) {
+                for (int b = 0; b < 64; ++b) {
+                    // widened to FP64 inside the store so that no FP64 pairs stay live across stores
+                    if (b < a.B)
+                        asm volatile("{\n\t.reg .f64 re, im;\n\tcvt.f64.f32 re, %1;\n\tcvt.f64.f32 im, %2;\n\t"
+                                     "st.global.cs.v2.f64 [%0], {re, im};\n\t}"
+                                     :: "l"(out), "f"(acc[b]), "f"(acc[64 + b]) : "memory");
+                    out += ld;
+                }
+            } else if (!HOST && row < a.n_out) {
                 float2* out = a.part + static_cast<int64_t>(kc) * a.B * a.n_out + row;
 #pragma unroll
                 for (int b = 0; b < 64; ++b)
@@ -692,6 +701,8 @@ cui_status phi_build(Plan& p) {
     if ((e = cudaFuncSetAttribute(phi_gemm_kernel<false, kFwdKS, kFwdNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sf))) != cudaSuccess ||
         (e = cudaFuncSetAttribute(phi_gemm_kernel<true, kAdjKS, kAdjNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(sa))) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(phi_gemm_kernel<true, kAdjKS, kAdjNS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(sa))) != cudaSuccess)
         return check_cuda(e, "cudaFuncSetAttribute");
     return CUI_OK;
@@ -766,9 +777,11 @@ cudaError_t launch_adj_phi(Plan* p, const float2* u, int64_t ldu, int B, cudaStr
     if ((e = timing_begin(p, 1, st)) != cudaSuccess) return e;
     CUtensorMap tmap;
     std::memcpy(&tmap, p->phi_tmap, sizeof tmap);
-    phi_gemm_kernel<true, kAdjKS, kAdjNS>
-        <<<dim3(static_cast<unsigned>(p->phi_npb / 32), p->phi_adj_kc), kPhiThreads, PhiCfg<kAdjKS, kAdjNS>::SMEM, st>>>(
-            a, tmap);
+    const dim3 grid(static_cast<unsigned>(p->phi_npb / 32), p->phi_adj_kc);
+    if (to_host)
+        phi_gemm_kernel<true, kAdjKS, kAdjNS, true><<<grid, kPhiThreads, PhiCfg<kAdjKS, kAdjNS>::SMEM, st>>>(a, tmap);
+    else
+        phi_gemm_kernel<true, kAdjKS, kAdjNS><<<grid, kPhiThreads, PhiCfg<kAdjKS, kAdjNS>::SMEM, st>>>(a, tmap);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = timing_end(p, st)) != cudaSuccess) return e;
