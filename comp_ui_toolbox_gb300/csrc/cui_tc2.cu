@@ -149,12 +149,15 @@ struct Fwd2Args {
 
 template <int NT>
 struct FwdCfg {
-    static constexpr int NS = NT >= 64 ? 2 : (NT >= 32 ? 3 : 4);  // B stages
-    static constexpr int NR = 4;                 // raw stages
+    // 16-column tiles run three blocks per SM: two B stages, three raw stages, a quarter of tensor
+    // memory and at most 64 registers a thread
+    static constexpr bool THREE = NT <= 16;
+    static constexpr int NS = NT >= 64 ? 2 : (NT >= 32 ? 3 : (THREE ? 2 : 4));  // B stages
+    static constexpr int NR = THREE ? 3 : 4;     // raw stages
     static constexpr int STB = NT * 1024;        // 4NT rows x 64 points x 4 B
     static constexpr int SBO = 2048;             // 8-row groups: 16 K groups x 128 B
-    // accumulators of 4NT columns; 16-column blocks run two per SM and take half of tensor memory each
-    static constexpr uint32_t TCOLS = NT >= 32 ? 512 : 256;
+    // accumulators of 4NT columns
+    static constexpr uint32_t TCOLS = NT >= 32 ? 512 : (THREE ? 128 : 256);
     static constexpr int NACC = TCOLS / (4 * NT);
     static constexpr int ITEMS = NT / 16;        // (4 points, column) items per producer
     static constexpr int LAG = NS - 1;           // read-out trails staging by LAG stages
@@ -175,7 +178,7 @@ struct FwdLayout {
 };
 
 template <int NT>
-__global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a) {
+__global__ void __launch_bounds__(kThreads2, FwdCfg<NT>::THREE ? 3 : 1) fwd_tc2_kernel(const Fwd2Args a) {
     using C = FwdCfg<NT>;
     extern __shared__ __align__(1024) unsigned char smem[];
     const FwdLayout<NT> L(a.ms, a.Bt, a.RBW);
@@ -514,7 +517,8 @@ __global__ void __launch_bounds__(kThreads2, 1) fwd_tc2_kernel(const Fwd2Args a)
 // fields of the unit from the slot-major residue copy (p_ad[f][z][r][slot of
 // f][j], one copy per unit) and keeps gamma_hat of its points in registers for
 // the whole frequency chunk.  A block covers L grid lines (2 with 64-column
-// tiles, whose single 128 KB B buffer is then reloaded once per 8 units).
+// tiles, whose single 128 KB B buffer is then reloaded once per 8 units, and
+// with 16-column tiles, which run two blocks per SM with one 32 KB B buffer).
 // ---------------------------------------------------------------------------
 
 // V tiles in the B-operand layout: vs[f][tile][4NT rows x 2Epad bf16], rows
@@ -572,16 +576,20 @@ struct Adj2Args {
 
 template <int NT>
 struct AdjCfg {
-    static constexpr int NB = NT >= 64 ? 1 : 2;  // V tile buffers (128 KB each at 64 columns)
+    // 16-column tiles run two blocks per SM, each with half of tensor memory, one V tile buffer
+    // shared by two grid lines and at most 102 registers a thread
+    static constexpr bool TWO = NT <= 16;
+    static constexpr int NB = (NT >= 64 || TWO) ? 1 : 2;  // V tile buffers (128 KB each at 64 columns)
     static constexpr int NA = 3;                 // spread-chunk stages
-    static constexpr int NP = 3;                 // incident-field stages
-    static constexpr int NACC = 512 / (4 * NT);  // accumulators of 4NT columns: all of tensor memory
-    static constexpr uint32_t TCOLS = 512;
+    static constexpr int NP = TWO ? 2 : 3;       // incident-field stages
+    static constexpr uint32_t TCOLS = TWO ? 256 : 512;
+    static constexpr int NACC = TCOLS / (4 * NT);  // accumulators of 4NT columns: all of the block's tensor memory
     static constexpr int LAG = 2;                // shared roles: the epilogue trails the spreading by 2 units
     // 16/32-column tiles: warps 0-3 spread the A operand and warps 4-7 run the epilogues, each
     // group at its own pace (the epilogue of a unit may trail its MMAs by up to NACC units)
     static constexpr bool SPLIT = NT <= 32;
-    static constexpr int MAXL = 2;               // grid lines per block
+    static constexpr int MAXL = 2;               // grid lines per block, at most
+    static constexpr int LINES = (NT >= 64 || TWO) ? MAXL : 1;
 };
 
 template <int NT>
@@ -604,7 +612,7 @@ struct AdjLayout {  // byte offsets of the dynamic shared memory
 };
 
 template <int NT>
-__global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a) {
+__global__ void __launch_bounds__(kThreads2, AdjCfg<NT>::TWO ? 2 : 1) adj_tc2_kernel(const Adj2Args a) {
     using C = AdjCfg<NT>;
     extern __shared__ __align__(1024) unsigned char smem[];
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
@@ -896,8 +904,9 @@ __global__ void __launch_bounds__(kThreads2, 1) adj_tc2_kernel(const Adj2Args a)
             }
         }
         if (!ok) atomicOr(a.status, 4);
-        // every MMA has completed (the last epilogue waited on it): the V buffers now hold the
-        // partial gamma_hat of each (column half, pass): sG[hc*NPS + ps][zi][x]
+        // every MMA has completed (the last epilogue waited on it) and every copy has been consumed:
+        // the stage buffers from offset 0 now hold the partial gamma_hat of each (column half, pass),
+        // sG[hc*NPS + ps][zi][x] (the host checks that it ends before the barriers)
         producers_sync();
         float2* sG = reinterpret_cast<float2*>(smem);
         const bool good = !*abort_flag;
@@ -1064,7 +1073,7 @@ cudaError_t launch_fwd2(Plan* p, const float2* gamma, int64_t ldg, int B, const 
 
 template <int NT>
 cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nfc_out) {
-    const int Lz = (NT >= 64) ? AdjCfg<NT>::MAXL : 1;  // grid lines per block
+    const int Lz = AdjCfg<NT>::LINES;  // grid lines per block
     const int zblocks = (p->Nz + Lz - 1) / Lz;
     const size_t slab = static_cast<size_t>(B) * p->P * sizeof(float2);
     const int target = p->tune_adj_blocks > 0 ? p->tune_adj_blocks : 8 * 152;  // blocks per launch
@@ -1086,6 +1095,12 @@ cudaError_t launch_adj2(Plan* p, int B, const Tile2& t, cudaStream_t st, int* nf
     a.Nx = p->Nx; a.Nz = p->Nz; a.Ex = p->Ex; a.E = p->E; a.Epad = p->Epad; a.B = B; a.Bt = t.Bt; a.F = p->F;
     a.fchunk = fchunk; a.ms = p->ms; a.L = Lz; a.P = p->P; a.part = p->ws_part; a.status = p->ws_status; a.wait_ns = p->wait_limit_ns;
     const AdjLayout<NT> L(a.Epad, a.RBW, a.ms, a.Jp, a.fchunk);
+    {   // the final gamma_hat sums staged over the stage buffers must end before the barriers
+        using C = AdjCfg<NT>;
+        constexpr int NH = C::SPLIT ? NT : NT / 2, MW = C::SPLIT ? NT / 2 : (NH < 16 ? NH : 16);
+        const size_t sg = sizeof(float2) * (C::SPLIT ? 1 : 2) * (NH / MW) * static_cast<size_t>(Lz) * p->Nx;
+        if (sg > static_cast<size_t>(L.oBar)) return cudaErrorInvalidValue;
+    }
     if ((e = cudaFuncSetAttribute(adj_tc2_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(L.total))) != cudaSuccess)
         return e;
@@ -1127,7 +1142,7 @@ bool tc2_supported(const Plan* p, std::string* why) {
     if (p->Ex > 128) { *why = "line-unit kernels cover up to 128 elements"; return false; }
     if (p->Nx % 8 != 0 || p->Nx > 512) { *why = "line-unit kernels need a lateral grid of 8..512 points, a multiple of 8"; return false; }
     if (p->max_slots_per_f > 32) { *why = "line-unit kernels cover up to 32 incident waves per frequency"; return false; }
-    // the adjoint's final gamma_hat halves (2 x Nx) reuse its two V buffers (2 x 16 NT Epad bytes)
+    // the 32-column adjoint's final gamma_hat halves (2 x Nx) reuse its two V buffers (2 x 16 NT Epad bytes)
     if (16 * p->Nx > 32 * 16 * ((p->Ex + 15) / 16 * 16)) {
         *why = "lateral grid too wide for the element count of the line-unit kernels";
         return false;
