@@ -775,7 +775,8 @@ int pick_nc(int slots) {
     if (slots <= 1) return 1;
     if (slots <= 2) return 2;
     if (slots <= 4) return 4;
-    if (slots <= 6) return 6;  // 5-6 waves (the 3D workload has 5): 8 would waste 3 of 8 columns
+    if (slots <= 5) return 5;  // the 3D workload's 5 waves: 6 would waste 1 of 6 columns, 8 3 of 8
+    if (slots <= 6) return 6;
     if (slots <= 8) return 8;
     if (slots <= 12) return 12;
     return 16;
@@ -1234,6 +1235,7 @@ cudaError_t run_forward(Plan* p, const float2* gamma, int64_t ldg, int B, float2
             case 1: e = launch_fwd<1>(p, gamma, ldg, B, st, occ_sel); break;
             case 2: e = launch_fwd<2>(p, gamma, ldg, B, st, occ_sel); break;
             case 4: e = launch_fwd<4>(p, gamma, ldg, B, st, occ_sel); break;
+            case 5: e = launch_fwd<5>(p, gamma, ldg, B, st, occ_sel); break;
             case 6: e = launch_fwd<6>(p, gamma, ldg, B, st, occ_sel); break;
             case 8: e = launch_fwd<8>(p, gamma, ldg, B, st, occ_sel); break;
             case 12: e = launch_fwd<12>(p, gamma, ldg, B, st, occ_sel); break;
@@ -1344,6 +1346,7 @@ cudaError_t run_adjoint(Plan* p, const float2* u, int64_t ldu, int B, float2* g,
         case 1: e = launch_adj<1>(p, B, st); break;
         case 2: e = launch_adj<2>(p, B, st); break;
         case 4: e = launch_adj<4>(p, B, st); break;
+        case 5: e = launch_adj<5>(p, B, st); break;
         case 6: e = launch_adj<6>(p, B, st); break;
         case 8: e = launch_adj<8>(p, B, st); break;
         case 12: e = launch_adj<12>(p, B, st); break;
@@ -1572,6 +1575,7 @@ extern "C" cui_status cui_born_forward_static(cui_born_plan* plan, const cui_com
         case 1: e = launch_fwd_static<1>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 2: e = launch_fwd_static<2>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 4: e = launch_fwd_static<4>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
+        case 5: e = launch_fwd_static<5>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 6: e = launch_fwd_static<6>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 8: e = launch_fwd_static<8>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
         case 12: e = launch_fwd_static<12>(p, reinterpret_cast<const float2*>(gamma), ld_gamma, n_objects, part, groups, lines_per_group, st); break;
