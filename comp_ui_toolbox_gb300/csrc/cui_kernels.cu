@@ -94,6 +94,36 @@ __device__ __forceinline__ void stage_row(float2* sA, const float2* __restrict__
         stage_band(sA, table + ((static_cast<int64_t>(f - tab_f0) * g.Nz + z) * g.Noy + oy) * g.Nox, g);
 }
 
+// Skewed band layout of the FP32 adjoint: entry n of the staged bands sits at n + n/16.  Its lanes
+// read the bands KJ entries apart; at an even KJ (the 2D arrays' 4) every fourth lane would hit the
+// same shared-memory bank, and one padding entry per 16 spreads them over all banks.
+template <bool SKEW>
+__device__ __forceinline__ int band_at(int n) { return SKEW ? n + (n >> 4) : n; }
+__host__ __device__ constexpr size_t band_capacity(size_t n) { return n + (n >> 4) + 1; }
+
+template <bool GEN, bool SKEW>
+__device__ __forceinline__ void stage_row_at(float2* sA, int off, const float2* __restrict__ table, int tab_f0,
+                                             const TableGen& t, int f, int z, int oy, const LineGeom& g) {
+    const int n = g.ppx * g.Ni;
+    if constexpr (GEN) {
+        const GenRow row = gen_row(t, f, z, oy);
+        for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+            const int r = idx / g.Ni;
+            const int i = idx - r * g.Ni - kPad;
+            const int o = r + g.ppx * i;
+            sA[band_at<SKEW>(off + idx)] = (i >= 0 && o < g.Nox) ? gen_entry(t, row, o) : make_float2(0.f, 0.f);
+        }
+    } else {
+        const float2* __restrict__ rowp = table + ((static_cast<int64_t>(f - tab_f0) * g.Nz + z) * g.Noy + oy) * g.Nox;
+        for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+            const int r = idx / g.Ni;
+            const int i = idx - r * g.Ni - kPad;
+            const int o = r + g.ppx * i;
+            sA[band_at<SKEW>(off + idx)] = (i >= 0 && o < g.Nox) ? __ldg(rowp + o) : make_float2(0.f, 0.f);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // dense forward: block = (line group x ey, frequency, object x column pass)
 // ---------------------------------------------------------------------------
@@ -524,8 +554,9 @@ __device__ __forceinline__ void adj_dense_body(const AdjArgs& a) {
     // V rows padded to an odd number of columns: lane groups reading elements espan apart then hit
     // different banks
     constexpr int NCP = NC | 1;
-    float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of EB element rows
-    float2* sV = sA + EB * g.ppx * g.Ni;             // [EB][Ex][NCP]
+    constexpr bool SKEW = (KJ % 2) == 0;
+    float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of EB element rows (skewed)
+    float2* sV = sA + band_capacity(static_cast<size_t>(EB) * g.ppx * g.Ni);  // [EB][Ex][NCP]
     float2* sR = sV + EB * g.Ex * NCP;               // [Nx]
     __shared__ int sSlot[NC];
 
@@ -574,7 +605,7 @@ __device__ __forceinline__ void adj_dense_body(const AdjArgs& a) {
                 if (threadIdx.x < NC) sSlot[threadIdx.x] = (threadIdx.x < nc) ? a.f_slot_list[s0 + c0 + threadIdx.x] : 0;
                 for (int k = 0; k < neb; ++k) {
                     const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
-                    stage_row<GEN>(sA + k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
+                    stage_row_at<GEN, SKEW>(sA, k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
                 }
                 __syncthreads();
                 for (int idx = threadIdx.x; idx < neb * NC * g.Ex; idx += blockDim.x) {
@@ -587,12 +618,12 @@ __device__ __forceinline__ void adj_dense_body(const AdjArgs& a) {
                 __syncthreads();
                 if (lane_on) {
                     for (int k = 0; k < neb; ++k) {
-                        const float2* Ar = sA + k * g.ppx * g.Ni + r * g.Ni + kPad;
+                        const int a0 = k * g.ppx * g.Ni + r * g.Ni + kPad;  // band r of row k
                         const float2* sVk = sV + k * g.Ex * NCP;
-                        int base = j0 - elo + g.Ex - 1;
+                        int base = a0 + j0 - elo + g.Ex - 1;
                         float2 win[KJ];
 #pragma unroll
-                        for (int t = 0; t < KJ; ++t) win[t] = Ar[base + t];
+                        for (int t = 0; t < KJ; ++t) win[t] = sA[band_at<SKEW>(base + t)];
                         for (int e = elo; e < ehi; ++e) {
                             const float2* vx = sVk + e * NCP;
                             float2 v[NC];
@@ -605,7 +636,7 @@ __device__ __forceinline__ void adj_dense_body(const AdjArgs& a) {
 #pragma unroll
                             for (int t = KJ - 1; t > 0; --t) win[t] = win[t - 1];
                             --base;
-                            win[0] = Ar[base];
+                            win[0] = sA[band_at<SKEW>(base)];
                         }
                     }
                 }
@@ -667,11 +698,14 @@ __global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_gen_kernel(const AdjA
     adj_dense_body<NC, KJ, true>(a);
 }
 
-// 3D setups with a stored or streamed table (see fwd_dense3_kernel): 237 vs 246 ms on the 3D array.
-// 2D setups where the ceiling is 128: 2d-batched FP32 adjoint 802 -> 713 ms, 2d-gradient 14.4 -> 13.2
-// ms; the single-wave 2d-plain adjoint is slower under a ceiling (0.28 -> 0.36 ms) and keeps the bound.
+// 3D setups with a stored or streamed table (see fwd_dense3_kernel) and 2D setups where the ceiling is
+// 128 (2d-batched FP32 adjoint 802 -> 713 ms, 2d-gradient 14.4 -> 13.2 ms; the single-wave 2d-plain
+// adjoint is slower under a ceiling, 0.28 -> 0.36 ms, and keeps the bound).  The 3D windows of fewer
+// than 24 accumulators take the lowest ceiling without spills: 64 registers below 16 accumulators (5
+// blocks of 192 threads per SM), else 80 (4 blocks); the 3D array's <5,3> adjoint went from 195.2 ms
+// (112 registers, 3 blocks) to 181.4 ms.
 template <int NC, int KJ>
-__global__ void __maxnreg__(NC * KJ >= 24 ? 128 : 112) adj_dense3_kernel(const AdjArgs a) {
+__global__ void __maxnreg__(NC * KJ >= 24 ? 128 : (NC * KJ >= 16 ? 80 : 64)) adj_dense3_kernel(const AdjArgs a) {
     adj_dense_body<NC, KJ, false>(a);
 }
 
@@ -1403,7 +1437,7 @@ size_t fwd_smem_bytes(const Plan* p, int nc) {
 
 size_t adj_smem_bytes(const Plan* p, int nc) {
     const size_t eb = adj_eyb(p);
-    return sizeof(float2) * (eb * p->ppx * p->Ni + eb * p->Ex * (nc | 1) + static_cast<size_t>(p->Nx));
+    return sizeof(float2) * (band_capacity(eb * p->ppx * p->Ni) + eb * p->Ex * (nc | 1) + static_cast<size_t>(p->Nx));
 }
 
 cui_status forward_device(Plan* p, const float2* gamma, int64_t ldg, int B, float2* u, int64_t ldu, cudaStream_t st) {
