@@ -95,31 +95,40 @@ dim3 host_grid(int64_t rows, int B) {
 
 // device staging columns (both paths) and, for the staging path, the pinned host buffers
 cui_status ensure_device_stage(Plan& p) {
-    if (p.d_stage_in) return CUI_OK;
-    const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
     cudaError_t e;
+    if (!p.in_stream && (e = cudaStreamCreateWithFlags(&p.in_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return check_cuda(e, "cudaStreamCreate");
+    if (!p.in_done && (e = cudaEventCreateWithFlags(&p.in_done, cudaEventDisableTiming)) != cudaSuccess)
+        return check_cuda(e, "cudaEventCreate");
+    // each buffer once; after a failed allocation the next call allocates the missing ones
+    const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
     void* v = nullptr;
     for (float2** d : {&p.d_stage_in, &p.d_stage_out, &p.d_stage_aux}) {
+        if (*d) continue;
         if ((e = cudaMalloc(&v, n * sizeof(float2))) != cudaSuccess) return check_cuda(e, "cudaMalloc");
         p.allocations.push_back(v);
         *d = static_cast<float2*>(v);
     }
-    if ((e = cudaMalloc(&v, sizeof(float) * p.max_objects)) != cudaSuccess) return check_cuda(e, "cudaMalloc");
-    p.allocations.push_back(v);
-    p.d_stage_loss = static_cast<float*>(v);
+    if (!p.d_stage_loss) {
+        if ((e = cudaMalloc(&v, sizeof(float) * p.max_objects)) != cudaSuccess) return check_cuda(e, "cudaMalloc");
+        p.allocations.push_back(v);
+        p.d_stage_loss = static_cast<float*>(v);
+    }
     return CUI_OK;
 }
 
 cui_status ensure_stage(Plan& p) {
     cui_status s = ensure_device_stage(p);
-    if (s != CUI_OK || p.h_stage_in) return s;
+    if (s != CUI_OK) return s;
     const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
-    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_in), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
-    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_out), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
-    e = cudaHostAlloc(reinterpret_cast<void**>(&p.h_stage_aux), n * sizeof(float2), cudaHostAllocDefault);
-    if (e != cudaSuccess) return check_cuda(e, "cudaHostAlloc");
+    for (float2** h : {&p.h_stage_in, &p.h_stage_out, &p.h_stage_aux}) {
+        if (*h) continue;  // after a failed allocation the next call allocates the missing ones
+        const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(h), n * sizeof(float2), cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            *h = nullptr;
+            return check_cuda(e, "cudaHostAlloc");
+        }
+    }
     p.h_stage_elems = n;
     return CUI_OK;
 }
@@ -239,12 +248,21 @@ cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, in
         cui_status s = ensure_device_stage(p);
         if (s != CUI_OK) return s;
         host_in_kernel<<<host_grid(p.P, n_objects), 256>>>(gamma, ld_gamma, p.P, p.d_stage_in);
-        host_in_kernel<<<host_grid(p.n_obs, n_objects), 256>>>(u_meas, ld_u, p.n_obs, p.d_stage_aux);
+        // the measured data are read on the plan's input stream while the forward runs; the previous
+        // call's residual, the last reader of d_stage_aux, ended before that call returned
+        host_in_kernel<<<host_grid(p.n_obs, n_objects), 256, 0, p.in_stream>>>(u_meas, ld_u, p.n_obs, p.d_stage_aux);
         count_launch(2);
-        if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "host input");
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(p.in_done, p.in_stream);
+        // no return before the read of the caller's u_meas has ended
+        struct InputGuard {
+            cudaStream_t s;
+            ~InputGuard() { cudaStreamSynchronize(s); }
+        } input_guard{p.in_stream};
+        if (e != cudaSuccess) return check_cuda(e, "host input");
         bool written = false;  // the folded adjoint may write the caller's gradient itself
         s = vjp_device(&p, p.d_stage_in, p.P, p.d_stage_aux, p.n_obs, n_objects, p.d_stage_out, p.P, p.d_stage_loss, 0,
-                       HostOut{grad, ld_grad, &written});
+                       HostOut{grad, ld_grad, &written}, p.in_done);
         if (s != CUI_OK) return s;
         if (!written) {
             launch_host_out(p.d_stage_out, p.P, n_objects, grad, ld_grad);

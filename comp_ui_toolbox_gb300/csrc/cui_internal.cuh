@@ -125,6 +125,9 @@ struct Plan {
     float2* d_stage_out = nullptr;
     float2* d_stage_aux = nullptr;
     float* d_stage_loss = nullptr;
+    // the host VJP reads the measured data on this stream while the forward runs on the caller's
+    cudaStream_t in_stream = nullptr;  // non-blocking: no implicit order against the legacy stream
+    cudaEvent_t in_done = nullptr;     // recorded after that read; the residual waits on it
 
     // host copies kept after creation (launch planning, table builders)
     std::vector<int> h_f_slot_ptr, h_f_slot_list, h_slot_f;
@@ -258,8 +261,10 @@ cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* 
 // n_iter proximal-gradient LASSO iterations, gamma updated in place (no allocation, no synchronisation)
 cui_status lasso_device(Plan* p, float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B, float step,
                         const float* lambda, int n_iter, float* loss, cudaStream_t st);
+// um_ready: an event the residual waits on before it reads um (null: um is ready on st)
 cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
-                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho = HostOut{});
+                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho = HostOut{},
+                      cudaEvent_t um_ready = nullptr);
 
 // shared-memory bytes the contraction kernels request
 size_t fwd_smem_bytes(const Plan* p, int nc);

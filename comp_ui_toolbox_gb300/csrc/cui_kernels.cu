@@ -1450,9 +1450,10 @@ cui_status adjoint_device(Plan* p, const float2* u, int64_t ldu, int B, float2* 
 }
 
 cui_status vjp_device(Plan* p, const float2* gamma, int64_t ldg, const float2* um, int64_t ldu, int B,
-                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho) {
+                      float2* grad, int64_t ldgr, float* loss, cudaStream_t st, HostOut ho, cudaEvent_t um_ready) {
     cudaError_t e = run_forward(p, gamma, ldg, B, p->ws_r, p->n_obs, st);
     if (e != cudaSuccess) return check_cuda(e, "vjp forward");
+    if (um_ready && (e = cudaStreamWaitEvent(st, um_ready, 0)) != cudaSuccess) return check_cuda(e, "vjp wait");
     residual_kernel<<<dim3(kLossBlocks, B), 256, 0, st>>>(p->ws_r, p->n_obs, um, ldu, p->n_obs, p->ws_loss);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return check_cuda(e, "vjp residual");

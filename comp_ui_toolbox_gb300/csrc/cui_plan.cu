@@ -82,6 +82,10 @@ cudaError_t upload(Plan& p, T** ptr, const std::vector<T>& h) {
 
 void free_plan(Plan& p) {
     timing_release(&p);
+    if (p.in_done) cudaEventDestroy(p.in_done);
+    if (p.in_stream) cudaStreamDestroy(p.in_stream);
+    p.in_done = nullptr;
+    p.in_stream = nullptr;
     for (void* v : p.allocations) cudaFree(v);
     p.allocations.clear();
     if (p.h_stage_in) cudaFreeHost(p.h_stage_in);
