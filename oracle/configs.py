@@ -110,6 +110,9 @@ def small_config(name: str) -> BornConfig:
         return BornConfig("c2-small", _setup_2d(64, 16, 16, LOSSLESS), np.linspace(2.5e6, 5.5e6, 8),
                           [Wave("rad", seed=200 + i) for i in range(4)], mixing="pm1", n_mixes=5,
                           mix_seed=210, n_objects=6, density=0.03, seed=13)
+    if name == "five":  # five waves per frequency: the FP32 kernels' 5-column instantiation
+        return BornConfig("five-small", _setup_2d(64, 24, 16, TISSUE), np.linspace(2.0e6, 6.0e6, 8),
+                          [Wave("qpw", (a,)) for a in (-8.0, -4.0, 0.0, 4.0, 8.0)], density=0.05, seed=16)
     if name == "ragged":  # uneven frequency subsets per wave and per mix
         f = np.linspace(2.5e6, 5.5e6, 10)
         waves = [Wave("qpw", (-6.0,), f_subset=np.array([0, 1, 2, 3, 5, 7, 9])),

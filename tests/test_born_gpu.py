@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5          # relative L2 vs FP64 oracle
 TOL_DOT = 1e-6      # dot-product (adjointness) test, relative to |Phi x| |y|
 
-CONFIGS = ["c0", "c1", "c2", "ragged", "c3"]
+CONFIGS = ["c0", "c1", "c2", "ragged", "c3", "five"]
 _BUILT = {}
 
 
@@ -454,6 +454,34 @@ def test_bf16x3_wide_tiles_partial_tile_and_odd_lines(n_lines, n_obj):
     w.n_points_axis = (w.n_points_axis[0], n_lines)
     op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
     rng = np.random.default_rng(5)
+    g = rng.standard_normal((op.n_points, n_obj)) + 1j * rng.standard_normal((op.n_points, n_obj))
+    y = rng.standard_normal((op.n_observations, n_obj)) + 1j * rng.standard_normal((op.n_observations, n_obj))
+    u32 = op.forward(dev(g)).cpu().numpy()
+    a32 = op.adjoint(dev(y)).cpu().numpy()
+    op.set_precision("bf16x3")
+    u16 = op.forward(dev(g)).cpu().numpy()
+    a16 = op.adjoint(dev(y)).cpu().numpy()
+    assert op.device_status() == 0
+    for b in range(n_obj):
+        assert rel_l2(u16[:, b], u32[:, b]) <= TOL
+        assert rel_l2(a16[:, b], a32[:, b]) <= TOL
+    op.close()
+
+
+@pytest.mark.parametrize("wname,n_lines,n_obj", [("2d-gradient", 9, 1), ("2d-gradient", 17, 1), ("2d-plain", 9, 3)])
+def test_bf16x3_narrow_tiles_odd_lines(wname, n_lines, n_obj):
+    """16-column tiles, whose adjoint blocks cover two grid lines (two blocks per SM): an odd
+    number of lines leaves the last block one line.  11 waves and one object fill 11 of 16
+    columns; one wave and three objects give two-object tiles, the last one half empty.
+    Compared per object with the FP32 path of the same plan; bound 1e-5."""
+    from comp_ui_toolbox_gb300 import OperatorBorn
+    from comp_ui_toolbox_gb300.workloads import workload
+
+    w = workload(wname)
+    w.f = w.f[:3]
+    w.n_points_axis = (w.n_points_axis[0], n_lines)
+    op = OperatorBorn.from_setup(**w.setup_kwargs(), device=0, max_objects=n_obj)
+    rng = np.random.default_rng(7)
     g = rng.standard_normal((op.n_points, n_obj)) + 1j * rng.standard_normal((op.n_points, n_obj))
     y = rng.standard_normal((op.n_observations, n_obj)) + 1j * rng.standard_normal((op.n_observations, n_obj))
     u32 = op.forward(dev(g)).cpu().numpy()
