@@ -94,9 +94,10 @@ __device__ __forceinline__ void stage_row(float2* sA, const float2* __restrict__
         stage_band(sA, table + ((static_cast<int64_t>(f - tab_f0) * g.Nz + z) * g.Noy + oy) * g.Nox, g);
 }
 
-// Skewed band layout of the FP32 adjoint: entry n of the staged bands sits at n + n/16.  Its lanes
-// read the bands KJ entries apart; at an even KJ (the 2D arrays' 4) every fourth lane would hit the
-// same shared-memory bank, and one padding entry per 16 spreads them over all banks.
+// Skewed band layout of the FP32 contractions: entry n of the staged bands sits at n + n/16.  Their
+// lanes read the bands one window (KJ or KE entries) apart; at an even window (the 2D arrays' 4)
+// lanes 16/window apart would hit the same shared-memory bank, and one padding entry per 16 spreads
+// them over all banks.
 template <bool SKEW>
 __device__ __forceinline__ int band_at(int n) { return SKEW ? n + (n >> 4) : n; }
 __host__ __device__ constexpr size_t band_capacity(size_t n) { return n + (n >> 4) + 1; }
@@ -152,8 +153,11 @@ __device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
     extern __shared__ float4 smem_f4[];
     const LineGeom& g = a.g;
     const int EB = a.eyb;
+    // lanes KE entries apart: the skewed band layout (band_at) at 4-entry windows (2d-plain forward
+    // 0.208 -> 0.180 ms); the 3D forward's 2-entry windows measured slower with it (172.8 -> 180.6 ms)
+    constexpr bool SKEW = (KE % 4) == 0;
     float2* sA = reinterpret_cast<float2*>(smem_f4);  // [EB][ppx * Ni] bands of the block's element rows
-    float2* sQ = sA + EB * g.ppx * g.Ni;             // [Nx][NC]
+    float2* sQ = sA + band_capacity(static_cast<size_t>(EB) * g.ppx * g.Ni);  // [Nx][NC]
     float2* sR = sQ + g.Nx * NC;                     // [EB][Ex][NC]
     __shared__ int sSlot[NC];
 
@@ -204,7 +208,7 @@ __device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
         __syncthreads();
         for (int k = 0; k < neb; ++k) {
             const int oy = iy - (ey0 + k) * g.ppy + (g.Ey - 1) * g.ppy;
-            stage_row<GEN>(sA + k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
+            stage_row_at<GEN, SKEW>(sA, k * g.ppx * g.Ni, a.table, a.tab_f0, a.gen, f, z, oy, g);
         }
         const float2* gam = a.gamma + static_cast<int64_t>(b) * a.ldg + pt0;
         for (int idx = threadIdx.x; idx < NC * g.Nx; idx += blockDim.x) {
@@ -215,11 +219,10 @@ __device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
         }
         __syncthreads();
         if (lane_on) {
-            const float2* Ar = sA + ek * g.ppx * g.Ni + r * g.Ni + kPad;
-            int base = jlo - e0 + g.Ex - 1;
+            int base = ek * g.ppx * g.Ni + r * g.Ni + kPad + jlo - e0 + g.Ex - 1;  // in band r of row ek
             float2 win[KE];
 #pragma unroll
-            for (int t = 0; t < KE; ++t) win[t] = Ar[base - t];
+            for (int t = 0; t < KE; ++t) win[t] = sA[band_at<SKEW>(base - t)];
             for (int j = jlo; j < jhi; ++j) {
                 const float2* qx = sQ + (r + g.ppx * j) * NC;
                 float2 q[NC];
@@ -232,7 +235,7 @@ __device__ __forceinline__ void fwd_dense_body(const FwdArgs& a) {
 #pragma unroll
                 for (int t = KE - 1; t > 0; --t) win[t] = win[t - 1];
                 ++base;
-                win[0] = Ar[base];
+                win[0] = sA[band_at<SKEW>(base)];
             }
         }
     }
@@ -1432,7 +1435,7 @@ void timing_release(Plan* p) {
 
 size_t fwd_smem_bytes(const Plan* p, int nc) {
     const size_t eb = fwd_rows_per_block(p->Ey);
-    return sizeof(float2) * (eb * p->ppx * p->Ni + static_cast<size_t>(p->Nx) * nc + eb * p->Ex * nc);
+    return sizeof(float2) * (band_capacity(eb * p->ppx * p->Ni) + static_cast<size_t>(p->Nx) * nc + eb * p->Ex * nc);
 }
 
 size_t adj_smem_bytes(const Plan* p, int nc) {
