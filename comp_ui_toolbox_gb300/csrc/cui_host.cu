@@ -102,18 +102,12 @@ cui_status ensure_device_stage(Plan& p) {
         return check_cuda(e, "cudaEventCreate");
     // each buffer once; after a failed allocation the next call allocates the missing ones
     const size_t n = static_cast<size_t>(std::max<int64_t>(p.P, p.n_obs)) * p.max_objects;
-    void* v = nullptr;
     for (float2** d : {&p.d_stage_in, &p.d_stage_out, &p.d_stage_aux}) {
         if (*d) continue;
-        if ((e = cudaMalloc(&v, n * sizeof(float2))) != cudaSuccess) return check_cuda(e, "cudaMalloc");
-        p.allocations.push_back(v);
-        *d = static_cast<float2*>(v);
+        const cui_status s = device_alloc(p, reinterpret_cast<void**>(d), n * sizeof(float2));
+        if (s != CUI_OK) return s;
     }
-    if (!p.d_stage_loss) {
-        if ((e = cudaMalloc(&v, sizeof(float) * p.max_objects)) != cudaSuccess) return check_cuda(e, "cudaMalloc");
-        p.allocations.push_back(v);
-        p.d_stage_loss = static_cast<float*>(v);
-    }
+    if (!p.d_stage_loss) return device_alloc(p, reinterpret_cast<void**>(&p.d_stage_loss), sizeof(float) * p.max_objects);
     return CUI_OK;
 }
 

@@ -9,7 +9,7 @@ switch that fails the same way must leave the plan working on its previous path.
 import numpy as np
 import pytest
 
-from oracle import configs, forward_quick_cpu
+from oracle import adjoint_quick_cpu, configs, forward_quick_cpu
 from tests.helpers import make_operator, rel_l2, setup_kwargs
 
 torch = pytest.importorskip("torch")
@@ -81,5 +81,39 @@ def test_failed_precision_switch_keeps_the_plan_working(precision, monkeypatch):
     assert failures >= 1
     assert op.precision == precision  # a later switch built what the failed ones could not
     assert rel_l2(op.forward(g).cpu().numpy(), u_ref) <= 1e-5
+    assert op.device_status() == 0
+    op.close()
+
+
+def test_failed_staging_allocation_then_host_vjp_succeeds(monkeypatch):
+    """The FP64 host entry points allocate their device staging buffers on first use.  Fail the
+    j-th of those allocations for j = 1, 2, ...: each failed call returns CUI_ERR_OOM, and the next
+    call on the same plan allocates only the buffers still missing.  The gradient of the call that
+    succeeds is the oracle's (bound 1e-5)."""
+    from comp_ui_toolbox_gb300 import CuiError
+    b = configs.build(configs.small_config("c1"))
+    op = make_operator(b, "lateral", max_objects=1)
+    gamma_true = configs.make_gamma(b.cfg)
+    u_meas = configs.add_noise(forward_quick_cpu(b.op, gamma_true), 30.0, seed=5)
+    gamma = np.random.default_rng(21).standard_normal(gamma_true.shape) + 0j
+    grad_ref = adjoint_quick_cpu(b.op, forward_quick_cpu(b.op, gamma) - u_meas)
+    failures = 0
+    for j in range(1, 20):
+        n0 = op.refresh_info()["device_allocations"]
+        monkeypatch.setenv("CUI_BORN_FAIL_ALLOC", str(n0 + j))
+        try:
+            grad, _ = op.vjp(gamma, u_meas)
+        except CuiError as e:
+            assert e.status == 3, e
+            assert "injected allocation failure" in str(e)
+            failures += 1
+            continue
+        finally:
+            monkeypatch.delenv("CUI_BORN_FAIL_ALLOC")
+        break
+    assert failures >= 1
+    assert rel_l2(np.asarray(grad), grad_ref) <= 1e-5
+    grad, _ = op.vjp(gamma, u_meas)  # the buffers are kept: no further allocation
+    assert rel_l2(np.asarray(grad), grad_ref) <= 1e-5
     assert op.device_status() == 0
     op.close()
