@@ -382,7 +382,10 @@ cui_status cui_born_lasso_host(cui_born_plan* plan, const cui_complex64* u_meas,
  * CUI_BORN_HOST_STAGING=1 before the first host call). */
 cui_status cui_born_host_path(cui_born_plan* plan, int32_t* direct);
 
-/* Host VJP: same as cui_born_vjp with host FP64 buffers; loss may be NULL. */
+/* Host VJP: same as cui_born_vjp with host FP64 buffers; loss may be NULL.
+ * Synchronous.  With the direct path, u_meas is read on a non-blocking stream
+ * the plan owns while the forward runs; the call returns only after that read
+ * has ended (also on errors), so the caller may free u_meas on return. */
 cui_status cui_born_vjp_host(cui_born_plan* plan, const cui_complex64* gamma, int64_t ld_gamma,
                              const cui_complex64* u_meas, int64_t ld_u, int32_t n_objects,
                              cui_complex64* grad, int64_t ld_grad, double* loss);
