@@ -873,7 +873,10 @@ AdjShape adj_shape(const Plan* p, int kj) {
 // Streamed table: the rows of frequencies f0 .. f0+nf-1 generated into the plan's chunk buffer
 // (layout [nf][Nz][Noy][Nox], like the stored table).  Block = rows, thread = lateral offset.
 __global__ void __launch_bounds__(256) table_chunk_kernel(const TableGen t, int f0, int n_rows, int Nz, int Noy,
-                                                          float2* __restrict__ out) {
+                                                          float2* __restrict__ out, const int* skip) {
+    // a forward's chunk is not needed when the occupancy pass chose the compacted forward, which
+    // generates its own entries (uniform over the grid)
+    if (skip && *skip != 0) return;
     for (int row = blockIdx.x; row < n_rows; row += gridDim.x) {
         const int oy = row % Noy, rz = row / Noy;
         const GenRow g = gen_row(t, f0 + rz / Nz, rz % Nz, oy);
@@ -882,10 +885,11 @@ __global__ void __launch_bounds__(256) table_chunk_kernel(const TableGen t, int 
     }
 }
 
-cudaError_t stream_table_chunk(const Plan* p, int f0, int nf, cudaStream_t st) {
+cudaError_t stream_table_chunk(const Plan* p, int f0, int nf, cudaStream_t st, const int* skip = nullptr) {
     const int n_rows = nf * p->Nz * p->Noy;
     const int threads = std::min(256, (p->Nox + 31) / 32 * 32);
-    table_chunk_kernel<<<std::min(n_rows, 152 * 16), threads, 0, st>>>(p->gen, f0, n_rows, p->Nz, p->Noy, p->stream_buf);
+    table_chunk_kernel<<<std::min(n_rows, 152 * 16), threads, 0, st>>>(p->gen, f0, n_rows, p->Nz, p->Noy, p->stream_buf,
+                                                                       skip);
     count_launch();
     return cudaGetLastError();
 }
@@ -916,7 +920,7 @@ cudaError_t launch_fwd_k(const Plan* p, const float2* gamma, int64_t ldg, int B,
     for (int f0 = 0; f0 < p->F; f0 += fstep) {
         const int nf = std::min(fstep, p->F - f0);
         if (p->table_mode == CUI_STORAGE_STREAMED) {
-            if ((e = stream_table_chunk(p, f0, nf, st)) != cudaSuccess) return e;
+            if ((e = stream_table_chunk(p, f0, nf, st, occ_sel)) != cudaSuccess) return e;
             a.table = p->stream_buf; a.f_base = f0; a.tab_f0 = f0;
         }
         kern<<<dim3(p->fwd_groups * a.n_eyb, nf, B * a.npass), sh.threads, smem, st>>>(a);
