@@ -232,7 +232,7 @@ def occupancy_sweep(op, densities=(0.001, 0.005, 0.02, 0.05, 0.0625, 0.1, 0.25, 
 def roofline_of(args, info, kt, B, clk, p_used: float = 1.0):
     """Roofline of the dominant contraction kernel of one apply.
 
-    Algorithmic work (the survey's work count): E = sum over slots of min(rows of the slot,
+    Algorithmic work (the channel-contraction work count): E = sum over slots of min(rows of the slot,
     distinct active elements) x P_used complex multiply-adds per object (``channel_macs``:
     the element sum folded into the receive mixes; P_used = the union occupancy of the
     forward's gamma columns, all points for the adjoint), x B objects.
