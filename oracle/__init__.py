@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library, its
 C-ABI or the Python host mirror) imports this package.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
-legs of ``bench.py`` use it, and only as the checker or the timed CPU
-baseline.
+legs of ``bench.py`` use it, and only to check the library's results or as
+the timed CPU baseline.
 
 The package restates, in numpy/scipy FP64, the reference toolbox's
 (mschiffn/comp_ui_toolbox) CPU Born operator and the table builders that

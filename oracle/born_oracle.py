@@ -1,7 +1,7 @@
 """FP64 restatement of the reference Born operator and its tables.
 
-TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): the checker for the
-CUDA library, never the thing measured or shipped.
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): the oracle the CUDA
+library's results are checked against, never the thing measured or shipped.
 
 All citations are paths inside the reference project
 (mschiffn/comp_ui_toolbox).  Conventions kept from the reference:

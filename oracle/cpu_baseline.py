@@ -1,7 +1,7 @@
 """Timed CPU baseline: the FP64 oracle operator on a bounded sample of a workload.
 
 TEST/BENCH INFRASTRUCTURE ONLY: used by ``bench.py``'s ``cpu_baseline`` leg
-(timed, and as the checker of the device path on the sample's rows) and by
+(timed, and to check the device path on the sample's rows) and by
 ``bench.py --impl reference``.  The reference's own CPU operator
 (MATLAB ``forward_quick_cpu`` / ``adjoint_quick_cpu``) cannot run on these
 machines; its restatement in :mod:`oracle.born_oracle` keeps the same loop

@@ -1,6 +1,6 @@
 """Frequency-split FP64 oracle for problems of the uneven-batch solver loop (test/bench infrastructure).
 
-TEST/BENCH INFRASTRUCTURE ONLY: used by ``tests/`` as the checker of the device LASSO iterations
+TEST/BENCH INFRASTRUCTURE ONLY: used by ``tests/`` to check the device LASSO iterations
 (``cui_born_lasso``) on problems of the uneven batch, and by ``bench.py``'s ``cpu_baseline`` leg of
 that workload.  Nothing in the product imports it.
 

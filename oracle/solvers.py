@@ -1,6 +1,6 @@
 """FP64 restatement of the solver loop that drives the Born operator (test infrastructure).
 
-TEST INFRASTRUCTURE ONLY: used by ``tests/`` as the checker of the library's
+TEST INFRASTRUCTURE ONLY: used by ``tests/`` to check the library's
 device LASSO iterations (``cui_born_lasso``) and orthogonal matching pursuit
 (``cui_born_omp``); nothing in the product imports it.
 
